@@ -1,0 +1,327 @@
+"""Benchmark: split-step KDK steps/s of the Schroedinger-Poisson solver on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+Default workload (N=1): 384^3, L = 40, complex FP32 psi, dt = dx^2/6, Strang KDK
+with the time-dependent Hernquist tidal tensor (host-integrated FP64 orbit) and
+1e5 static Plummer baryons CIC-deposited every step; seeded synthetic input.
+
+One JSON line is printed by rank 0:
+* value      steps/s with psi resident in HBM (one wdm_step_async call of K steps,
+             CUDA events on the library's stream; psi is 453 MB > L2 so no flush)
+* e2e        steps/s through the C ABI with host buffers: per step the pinned
+             host psi is copied in (wdm_set_psi), one step runs (wdm_step) and
+             psi is copied back (wdm_get_psi)
+* roofline   the dominant pass: its algorithmic bytes per launch / its mean
+             event-timed duration, against the measured HBM copy bandwidth
+* cpu_baseline  the FP64 oracle (numpy + scipy.fft, all host cores) on a
+             bounded sample of the same workload
+--impl reference times that CPU restatement alone (the reference is Julia and
+cannot run here; its FFTW CPU path is restated by the oracle).
+Under torchrun (N>1) every rank runs an independent replica (one halo per GPU;
+the path has no data exchange), value = total steps/s over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_ALG_PER_CELL = 192.0  # 4 C2C 3D FFTs x 3 axis passes x (8 B read + 8 B write) of complex64
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def setup_context(wdm, wl, phase_mode, steps_total):
+    N, L = wl["n"], wl["L"]
+    ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=wl["poisson_coeff"], phase_mode=phase_mode)
+    psi0 = wl["psi0"].astype(np.complex64)
+    ctx.set_psi(psi0)
+    if wl["tidal"] is not None:
+        ctx.set_tidal(wl["tidal"](np.arange(steps_total + 1) * wl["dt"]))
+    if wl["particles"] is not None:
+        ctx.set_particles(*wl["particles"])
+    return ctx, psi0
+
+
+def run_native(args, rank, world):
+    import torch
+
+    import wavedm_gb300 as wdm
+
+    wdm.build_library()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    wl = wdm.ics.workload(args.workload, n=args.n)
+    N, dt = wl["n"], wl["dt"]
+    K, W = args.steps, args.warmup
+    ctx, psi0 = setup_context(wdm, wl, args.phase, max(K, W, 1))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up (also builds the potential of psi0)
+    ctx.step(W, dt, mode=args.mode)
+    ctx.set_psi(psi0)
+    ctx.get_phi()  # potential of psi0 outside the timed region
+    ctx.set_tidal(wl["tidal"](np.arange(K + 1) * dt) if wl["tidal"] is not None else None)
+    ctx.set_profiling(True)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launch_count
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    ctx.step(K, dt, mode=args.mode, sync=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count - l0
+    clk = clocks.stop()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = K * world / (ms / 1e3)
+
+    # e2e: host psi in, one step, psi out, per step (pinned host buffers)
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.from_numpy(psi0.view(np.float32).reshape(-1)).pin_memory()
+        host_out = torch.empty_like(host_in).pin_memory()
+        ne = max(1, min(K, args.e2e_steps))
+        ctx.set_tidal(wl["tidal"](np.arange(2) * dt) if wl["tidal"] is not None else None)
+        import ctypes as C
+
+        lib = ctx.lib
+        for _ in range(2):
+            wdm._abi.check(lib.wdm_set_psi(ctx.handle, C.c_void_p(host_in.data_ptr()), 0), ctx.handle)
+            wdm._abi.check(lib.wdm_step(ctx.handle, 1, dt, 0.0, 0), ctx.handle)
+            wdm._abi.check(lib.wdm_get_psi(ctx.handle, C.c_void_p(host_out.data_ptr()), 0), ctx.handle)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            wdm._abi.check(lib.wdm_set_psi(ctx.handle, C.c_void_p(host_in.data_ptr()), 0), ctx.handle)
+            wdm._abi.check(lib.wdm_step(ctx.handle, 1, dt, 0.0, 0), ctx.handle)
+            wdm._abi.check(lib.wdm_get_psi(ctx.handle, C.c_void_p(host_out.data_ptr()), 0), ctx.handle)
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        nb = psi0.nbytes
+        e2e = {"value": ne * world / el, "unit": "steps/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+               "steps": ne, "calls_per_step": ["wdm_set_psi(host)", "wdm_step(1)", "wdm_get_psi(host)"]}
+    ctx.close()
+
+    # roofline of the dominant pass
+    peak, peak_kind = measured_peaks()
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    name, p = top
+    mean_ms = p["ms"] / max(p["launches"], 1)
+    achieved = p["bytes_per_launch"] / (mean_ms / 1e3) / 1e9
+    passes = {k: {"launches": v["launches"], "ms": round(v["ms"], 4),
+                  "share": round(v["ms"] / max(sum(q["ms"] for q in prof.values()), 1e-12), 4),
+                  "GBps": round(v["bytes_per_launch"] / (v["ms"] / max(v["launches"], 1) / 1e3) / 1e9, 1)}
+              for k, v in prof.items() if v["launches"]}
+    ncell = N ** 3
+    rec = {
+        "metric": f"KDK steps/s at {N}^3 (Strang, complex FP32 psi, {args.phase} phases)",
+        "value": round(value, 3),
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": round(ms / K, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64",
+        "data": "synthetic (seeded soliton + 4096-plane-wave NFW halo; Hernquist tide; 1e5 Plummer baryons)",
+        "config": {"workload": wl["name"], "grid": [N, N, N], "box": wl["L"], "dt": dt, "mode": args.mode,
+                   "phase_mode": args.phase, "tidal": wl["tidal"] is not None,
+                   "baryon_particles": 0 if wl["particles"] is None else len(wl["particles"][1]),
+                   "l2": "inputs larger than L2 (psi 8 B/cell)", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "bytes_per_launch": p["bytes_per_launch"], "mean_launch_ms": round(mean_ms, 5)},
+        "step_effective": {"B_alg_per_cell": B_ALG_PER_CELL,
+                           "GBps": round(B_ALG_PER_CELL * ncell * value / world / 1e9, 1),
+                           "frac_of_peak": round(B_ALG_PER_CELL * ncell * value / world / 1e9 / peak, 4)},
+        "passes": passes,
+        "gpu_launches": int(launches),
+        "e2e": e2e,
+        "clocks": clk,
+    }
+    return rec
+
+
+def oracle_setup(wl, nsteps):
+    from oracle import spe
+
+    N, L, dt = wl["n"], wl["L"], wl["dt"]
+    g = spe.Grid((N, N, N), (L, L, L))
+    rho_b = spe.cic_deposit(g, *wl["particles"]) if wl["particles"] is not None else None
+    sched = wl["tidal"](np.arange(nsteps + 2) * dt) if wl["tidal"] is not None else None
+    tidal = (lambda t: tuple(sched[int(round(t / dt))])) if sched is not None else None
+    phys = spe.Physics(poisson_coeff=wl["poisson_coeff"], rho_b=rho_b, tidal=tidal)
+    return spe, g, phys
+
+
+def time_oracle(wl, budget_s, max_steps, warm=1):
+    """FP64 oracle Strang steps on all host cores; returns (steps/s, steps timed, cores)."""
+    spe, g, phys = oracle_setup(wl, max_steps + warm)
+    dt = wl["dt"]
+    psi = wl["psi0"].astype(np.complex64).astype(np.complex128)
+    for s in range(warm):
+        psi = spe.kdk_step(psi, g, phys, s * dt, dt)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        psi = spe.kdk_step(psi, g, phys, (warm + n) * dt, dt)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return n / el, n, spe.WORKERS
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["native", "reference"], default="native")
+    ap.add_argument("--workload", type=int, default=3)
+    ap.add_argument("--n", type=int, default=None, help="override the grid size of the workload")
+    ap.add_argument("--phase", choices=["precise", "plain"], default="precise")
+    ap.add_argument("--mode", choices=["strang", "reference_loop", "lie"], default="strang")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of oracle time for cpu_baseline")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import wavedm_gb300 as wdm
+
+        wl = wdm.ics.workload(args.workload, n=args.n)
+        v, n, cores = time_oracle(wl, budget_s=150.0, max_steps=args.steps, warm=min(args.warmup, 1))
+        N = wl["n"]
+        sample = f"{n} timed FP64 Strang steps of the full {N}^3 workload after {min(args.warmup, 1)} warm-up"
+        print(json.dumps({
+            "impl": "reference",
+            "metric": f"KDK steps/s at {N}^3 (Strang, complex FP32 psi, {args.phase} phases)",
+            "value": round(v, 5), "unit": "steps/s", "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1),
+            "ms_per_step": round(1e3 / v, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic (same seeded workload)",
+            "config": {"workload": wl["name"], "grid": [N, N, N], "mode": "strang"},
+            "cpu_baseline": {"value": round(v, 5), "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": sample,
+                             "what": "oracle/spe.py: numpy/scipy.fft FP64 restatement of the reference's FFTW "
+                                     "CPU path (Julia absent)"},
+            "e2e": {"value": round(v, 5), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+        return
+
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    rec = run_native(args, rank, world)
+    if rank == 0 and not args.no_cpu_baseline:
+        import wavedm_gb300 as wdm
+
+        wl = wdm.ics.workload(args.workload, n=args.n)
+        v, n, cores = time_oracle(wl, budget_s=args.cpu_budget, max_steps=1000, warm=1)
+        rec["cpu_baseline"] = {"value": round(v, 5), "unit": "steps/s", "cores": cores, "kind": "port",
+                               "sample": f"{n} FP64 Strang steps of the full {wl['n']}^3 workload (1 warm-up)"}
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(rec), flush=True)
+
+
+if __name__ == "__main__":
+    main()

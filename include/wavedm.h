@@ -1,0 +1,147 @@
+/*
+ * libwavedm -- GB300 (sm_103a) split-step Fourier kick-drift-kick step for the
+ * Schroedinger-Poisson equation, behind a plain C ABI.
+ *
+ * Every entry point returns a wdm_status; wdm_last_error() gives the message of
+ * the last failure on a context (or the last create failure when ctx is NULL).
+ * The context owns every device buffer and one CUDA stream; host buffers passed
+ * in are borrowed for the duration of the call only.  Calls on one context are
+ * not thread safe (one context per host thread).  A call returns after its work
+ * is complete on the GPU unless its name ends in _async.
+ *
+ * Arrays are C order [nz][ny][nx] (x fastest), which is the memory order of the
+ * reference's column-major Julia arrays psi[x, y, z]: a Julia Array{ComplexF32,3}
+ * or CuArray{ComplexF32,3} is passed as is.
+ *
+ * Reference interfaces replaced (paths inside the WaveDM.jl project):
+ *   apply_kick_step!          src/solver/KDK.jl:37-77        -> wdm_kick
+ *   apply_drift_step!         src/solver/KDK.jl:88-101       -> wdm_drift
+ *   setup_fft_operators       src/solver/fft_operators.jl:8-15 -> built inside wdm_drift / wdm_step
+ *   setup_absorption_boundary src/solver/fft_operators.jl:22-27 -> wdm_desc.absorb_alpha
+ *   compute_gravitational_potential src/solver/gravity.jl:7-35 -> wdm_get_phi
+ *   parallel_poisson / _poisson_gpu src/parallel_poisson.jl:36-68 -> wdm_poisson
+ *   SPE3D_waveDM loop body    src/simulation_main.jl:536-559 -> wdm_step
+ *   add_tidal_potential!      src/physics/tidal_fields.jl:64-118 -> wdm_set_tidal
+ *   total mass / virial sums  src/simulation_main.jl:652, src/visualization/runtime.jl:210-238 -> wdm_reduce
+ */
+#ifndef WAVEDM_H
+#define WAVEDM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  WDM_OK = 0,
+  WDM_ERR_INVALID = 1,      /* bad argument (null pointer, size, mode)            */
+  WDM_ERR_UNSUPPORTED = 2,  /* grid size without an FFT plan, option not built    */
+  WDM_ERR_CUDA = 3,         /* a CUDA runtime call failed                         */
+  WDM_ERR_ALLOC = 4,        /* device allocation failed                           */
+  WDM_ERR_NONFINITE = 5,    /* psi or Phi holds NaN/Inf after a step              */
+  WDM_ERR_STATE = 6         /* call out of order (e.g. no psi set yet)            */
+} wdm_status;
+
+typedef enum { WDM_HOST = 0, WDM_DEVICE = 1 } wdm_where;
+
+typedef enum {
+  WDM_STEP_STRANG = 0,         /* K(dt/2) D(dt) [mask] K(dt/2), docs/src/algorithms.md:120-142 */
+  WDM_STEP_REFERENCE_LOOP = 1, /* K(dt/2) D(dt) [mask]: the literal loop, simulation_main.jl:538-547 */
+  WDM_STEP_LIE = 2             /* K(dt) D(dt) [mask]: KDK_flag = false                       */
+} wdm_step_mode;
+
+typedef enum {
+  WDM_GRID_PERIODIC = 0,  /* x_i = -L/2 + i L/N, k = 2 pi m / L                           */
+  WDM_GRID_REFERENCE = 1  /* x = LinRange(-L/2, L/2, N) (poisson.jl:8-15), k = 2 pi m / L  */
+} wdm_grid_convention;
+
+typedef enum {
+  WDM_PHASE_PLAIN = 0,    /* FP32 phases k^2 dt/2 and Phi dt                               */
+  WDM_PHASE_PRECISE = 1   /* FP64-built separable drift tables; kick phase reduced mod 2 pi
+                             in float-float before the FP32 sincos                          */
+} wdm_phase_mode;
+
+typedef struct {
+  int32_t nx, ny, nz;          /* grid points per axis: each 2^a 3^b with a plan (8..512)   */
+  double lx, ly, lz;           /* full box lengths                                          */
+  int32_t convention;          /* wdm_grid_convention                                       */
+  double poisson_coeff;        /* c in lap Phi = c (rho - <rho>): 4 pi G (4pi in the reference, gravity.jl:23) */
+  double kerr;                 /* kappa of the local potential kappa |psi|^2 (0: off)       */
+  double absorb_alpha;         /* absorbing-mask coefficient (0: no mask), fft_operators.jl:22-27 */
+  int32_t phase_mode;          /* wdm_phase_mode                                            */
+  int32_t batch;               /* independent halos of this size advanced together (>= 1)  */
+} wdm_desc;
+
+typedef struct wdm_ctx wdm_ctx;
+
+/* lifecycle ---------------------------------------------------------------- */
+wdm_status wdm_create(const wdm_desc* desc, wdm_ctx** out);
+wdm_status wdm_destroy(wdm_ctx* ctx);
+const char* wdm_last_error(const wdm_ctx* ctx);
+int32_t wdm_version(void);
+/* 1 when an FFT plan exists for n (2^a 3^b in [8, 512]) */
+int32_t wdm_size_supported(int32_t n);
+
+/* state --------------------------------------------------------------------- */
+/* psi: complex64 (interleaved float pairs) [batch][nz][ny][nx] */
+wdm_status wdm_set_psi(wdm_ctx* ctx, const void* psi, int32_t where);
+wdm_status wdm_get_psi(wdm_ctx* ctx, void* psi, int32_t where);
+/* rho = |psi|^2 and the total potential Phi (gravity only, no V/tide), float32 */
+wdm_status wdm_get_rho(wdm_ctx* ctx, float* rho, int32_t where);
+wdm_status wdm_get_phi(wdm_ctx* ctx, float* phi, int32_t where);
+/* static external potential V [batch][nz][ny][nx] float32; NULL clears it */
+wdm_status wdm_set_static_potential(wdm_ctx* ctx, const float* V, int32_t where);
+/* tidal tensor 1/2 x^T T x about the box centre, T = (xx, yy, zz, xy, xz, yz).
+ * schedule: nsched rows of 6 doubles, row s used by the kick at time t0 + s*dt of
+ * the next wdm_step (a row per batch item when nsched == batch and per_item != 0).
+ * nsched == 0 turns the tide off. */
+wdm_status wdm_set_tidal(wdm_ctx* ctx, const double* schedule, int32_t nsched, int32_t per_item);
+/* baryon particles (positions [n][3] and masses [n], doubles), CIC-deposited
+ * into the density before every Poisson solve; n == 0 removes them. */
+wdm_status wdm_set_particles(wdm_ctx* ctx, const double* pos, const double* mass, int64_t n);
+
+/* the path ------------------------------------------------------------------ */
+/* nsteps steps of size dt from time t0 */
+wdm_status wdm_step(wdm_ctx* ctx, int32_t nsteps, double dt, double t0, int32_t mode);
+wdm_status wdm_step_async(wdm_ctx* ctx, int32_t nsteps, double dt, double t0, int32_t mode);
+/* apply_kick_step!: Phi from |psi|^2, psi <- exp(-i dt (Phi + V + tide(t))) psi */
+wdm_status wdm_kick(wdm_ctx* ctx, double dt, double t);
+/* apply_drift_step!: psi <- mask * ifft(exp(-i k^2 dt/2) fft(psi)) */
+wdm_status wdm_drift(wdm_ctx* ctx, double dt);
+/* parallel_poisson: phi = Poisson(rho) with lap phi = coeff (rho - <rho>), float32
+ * [batch][nz][ny][nx] in and out (host or device pointers) */
+wdm_status wdm_poisson(wdm_ctx* ctx, const float* rho, float* phi, int32_t where);
+/* in-place 3D C2C FFT of a complex64 device array (dir = -1 forward, +1 inverse, unnormalised) */
+wdm_status wdm_fft3d(wdm_ctx* ctx, void* data_dev, int32_t dir);
+
+/* diagnostics --------------------------------------------------------------- */
+/* out[0..9] (per batch item, 10 doubles each): mass, rho_max, argmax (flat index),
+ * centre of mass x, y, z, and the virial sums VirialPotential, TotalKineticE,
+ * TotalQuantumE, Virial = 2K + 2Q - VirialPotential */
+wdm_status wdm_reduce(wdm_ctx* ctx, double* out);
+/* CIC interpolation of Phi (gravity) at n positions [n][3] -> out[n] (doubles, host) */
+wdm_status wdm_interpolate_phi(wdm_ctx* ctx, const double* pos, int64_t n, double* out);
+/* 1 if the last checked step left psi finite */
+wdm_status wdm_check_finite(wdm_ctx* ctx, int32_t* finite);
+/* CUDA stream the context runs on (a cudaStream_t) */
+void* wdm_stream(wdm_ctx* ctx);
+
+/* profiling ------------------------------------------------------------------ */
+/* per-pass GPU time: with on != 0 every pass launch is bracketed by CUDA events
+ * on the context stream (off by default; turning it on clears the totals) */
+wdm_status wdm_set_profiling(wdm_ctx* ctx, int32_t on);
+/* for pass p < WDM_NPASS: launches, summed milliseconds and algorithmic bytes
+ * (one read + one write of every operand) of one launch, since profiling on */
+wdm_status wdm_get_profile(wdm_ctx* ctx, int64_t* launches, double* ms, double* bytes_per_launch);
+/* number of passes and the name of pass p */
+int32_t wdm_num_passes(void);
+const char* wdm_pass_name(int32_t p);
+/* kernel launches issued by this context since creation */
+int64_t wdm_launch_count(const wdm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,21 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built libwavedm.so")
+
+
+@pytest.fixture(scope="session")
+def wdm():
+    """The package, with libwavedm.so built in-tree (fails loudly if it cannot be)."""
+    import wavedm_gb300
+
+    wavedm_gb300.build_library()
+    return wavedm_gb300

@@ -1,0 +1,230 @@
+"""CUDA path vs the FP64 oracle, through the C ABI (needs a GPU).
+
+Tolerances (relative L2, test/simulation_SPE3D_validation.jl:85-88):
+* single 3D FFTs                         2e-6 (FP32 rounding, ~eps log2 N)
+* Poisson solve                          2e-6
+* short runs on small grids (<= 8 steps) 2e-5
+* workload 1 (64^3, 100 Strang steps)    1e-5 for psi in the precise phase form,
+                                          mass conserved to 1e-6
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import spe
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _rand_c64(shape, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+FFT_SHAPES = [(8, 8, 8), (16, 12, 24), (32, 32, 32), (48, 64, 96), (128, 128, 128), (192, 16, 8), (256, 8, 16),
+              (384, 8, 8), (512, 8, 8), (8, 384, 16), (8, 16, 384), (64, 96, 12)]
+
+
+@pytest.mark.parametrize("n", FFT_SHAPES, ids=["x".join(map(str, s)) for s in FFT_SHAPES])
+def test_fft3d_matches_numpy(wdm, torch_cuda, n):
+    torch = torch_cuda
+    nx, ny, nz = n
+    for batch in (1, 2):
+        shape = (batch, nz, ny, nx)
+        x = _rand_c64(shape, seed=nx + 7 * ny + 13 * nz + batch)
+        with wdm.SPEContext(n, (1.0, 1.0, 1.0), batch=batch) as ctx:
+            d = torch.from_numpy(x).cuda()
+            ctx.fft3d(d)
+            got = d.cpu().numpy()
+            ref = np.fft.fftn(x.astype(np.complex128), axes=(1, 2, 3))
+            assert spe.rel_l2(got, ref) < 2e-6
+            ctx.fft3d(d, inverse=True)
+            back = d.cpu().numpy() / (nx * ny * nz)
+            assert spe.rel_l2(back, x) < 2e-6
+
+
+@pytest.mark.parametrize("n", [(16, 16, 16), (24, 12, 48), (64, 64, 64), (128, 96, 32)])
+def test_poisson_matches_oracle(wdm, n):
+    nx, ny, nz = n
+    L = (3.0, 2.0, 4.0)
+    rng = np.random.default_rng(5)
+    rho = rng.uniform(0.0, 2.0, size=(nz, ny, nx)).astype(np.float32)
+    with wdm.SPEContext(n, L, poisson_coeff=4 * np.pi) as ctx:
+        phi = ctx.poisson(rho)
+    g = spe.Grid(n, L)
+    ref = spe.poisson(rho.astype(np.float64), g, 4 * np.pi)
+    assert spe.rel_l2(phi, ref) < 2e-6
+
+
+def test_poisson_single_mode(wdm):
+    n, L = (32, 16, 8), (2.0, 1.0, 0.5)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    k = 2 * np.pi * np.array([3 / L[0], 1 / L[1], 2 / L[2]])
+    rho = (1.0 + np.cos(k[0] * X + k[1] * Y + k[2] * Z)) * np.ones((8, 16, 32))
+    with wdm.SPEContext(n, L, poisson_coeff=1.0) as ctx:
+        phi = ctx.poisson(rho.astype(np.float32))
+    expect = -(rho - 1.0) / np.dot(k, k)
+    assert np.abs(phi - expect).max() < 2e-6 * np.abs(expect).max()
+
+
+def _ctx_for_golden(wdm, d, phase_mode="precise"):
+    n = tuple(int(v) for v in d["n"])
+    L = tuple(float(v) for v in d["L"])
+    ctx = wdm.SPEContext(n, L, convention=str(d["convention"]), poisson_coeff=float(d["c"]), kerr=float(d["kerr"]),
+                         absorb_alpha=float(d["alpha"]), phase_mode=phase_mode)
+    ctx.set_psi(d["psi0"])
+    if "V" in d:
+        ctx.set_static_potential(d["V"])
+    if "tidal" in d:
+        ctx.set_tidal(d["tidal"])
+    if "pos" in d:
+        ctx.set_particles(d["pos"], d["mass"])
+    return ctx
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(f)[:-4] for f in GOLDEN])
+@pytest.mark.parametrize("phase_mode", ["precise", "plain"])
+def test_step_matches_golden(wdm, path, phase_mode):
+    d = dict(np.load(path))
+    with _ctx_for_golden(wdm, d, phase_mode) as ctx:
+        ctx.step(int(d["steps"]), float(d["dt"]), mode=str(d["mode"]))
+        psi = ctx.get_psi()
+        phi = ctx.get_phi()
+    assert spe.rel_l2(psi, d["psi"]) < 2e-5
+    assert spe.rel_l2(phi, d["phi"]) < 2e-5
+
+
+@pytest.mark.parametrize("path", GOLDEN[:2], ids=[os.path.basename(f)[:-4] for f in GOLDEN[:2]])
+def test_step_in_pieces_equals_one_call(wdm, path):
+    """Several wdm_step calls chain like one (the potential stays valid across calls)."""
+    d = dict(np.load(path))
+    if "tidal" in d:
+        pytest.skip("schedule rows are per call")
+    steps, dt = int(d["steps"]), float(d["dt"])
+    with _ctx_for_golden(wdm, d) as ctx:
+        for s in range(steps):
+            ctx.step(1, dt, t0=s * dt, mode=str(d["mode"]))
+        psi = ctx.get_psi()
+    assert spe.rel_l2(psi, d["psi"]) < 2e-5
+
+
+def test_kick_and_drift_match_oracle(wdm):
+    n, L = (32, 24, 16), (6.0, 5.0, 4.0)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    rng = np.random.default_rng(11)
+    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2)) * np.exp(1j * rng.uniform(0, 1, (16, 24, 32)))).astype(np.complex64)
+    phys = spe.Physics(poisson_coeff=3.0)
+    with wdm.SPEContext(n, L, poisson_coeff=3.0) as ctx:
+        ctx.set_psi(psi0)
+        ctx.kick(0.05)
+        k = ctx.get_psi()
+        ctx.drift(0.03)
+        dr = ctx.get_psi()
+    ref_k = spe.kick(psi0.astype(np.complex128), spe.potential(psi0.astype(np.complex128), g, phys, 0.0), 0.05)
+    assert spe.rel_l2(k, ref_k) < 2e-6
+    ref_d = spe.drift(ref_k, g, 0.03)
+    assert spe.rel_l2(dr, ref_d) < 4e-6
+
+
+def test_workload1_parity_and_mass(wdm):
+    """Workload 1: 64^3, L = 20, dt = dx^2/6, 100 Strang steps vs the complex128 oracle."""
+    w = wdm.ics.workload(1)
+    N, L, dt, steps = w["n"], w["L"], w["dt"], w["steps"]
+    psi0 = w["psi0"].astype(np.complex64)
+    g = spe.Grid((N, N, N), (L, L, L))
+    ref = spe.run(psi0.astype(np.complex128), g, spe.Physics(poisson_coeff=1.0), dt, steps)
+    errs = {}
+    for mode in ("precise", "plain"):
+        with wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=1.0, phase_mode=mode) as ctx:
+            ctx.set_psi(psi0)
+            m0 = ctx.reduce()["mass"]
+            ctx.step(steps, dt)
+            psi = ctx.get_psi()
+            rho = ctx.get_rho()
+            m1 = ctx.reduce()["mass"]
+        errs[mode] = spe.rel_l2(psi, ref)
+        assert abs(m1 / m0 - 1) < 1e-6
+        assert spe.rel_l2(rho, np.abs(ref) ** 2) < 2e-5
+    print("workload-1 psi rel-L2:", errs)
+    assert errs["precise"] <= 1e-5
+
+
+def test_batch_items_are_independent(wdm):
+    n, L = (16, 16, 16), (8.0, 8.0, 8.0)
+    rng = np.random.default_rng(2)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    psis = [(np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 + b)) * np.exp(1j * rng.uniform(0, 1, (16, 16, 16))))
+            .astype(np.complex64) for b in range(3)]
+    T = np.array([[0.02 * (b + 1), -0.01, -0.01, 0, 0, 0] for b in range(3)])
+    with wdm.SPEContext(n, L, poisson_coeff=2.0, batch=3) as ctx:
+        ctx.set_psi(np.stack(psis))
+        ctx.set_tidal(T, per_item=True)
+        ctx.step(4, 0.02)
+        out = ctx.get_psi()
+    for b in range(3):
+        phys = spe.Physics(poisson_coeff=2.0, tidal=lambda t, b=b: tuple(T[b]))
+        ref = spe.run(psis[b].astype(np.complex128), g, phys, 0.02, 4)
+        assert spe.rel_l2(out[b], ref) < 2e-5
+
+
+def test_reductions_match_oracle(wdm):
+    d = dict(np.load(GOLDEN[0]))
+    n = tuple(int(v) for v in d["n"])
+    L = tuple(float(v) for v in d["L"])
+    with _ctx_for_golden(wdm, d) as ctx:
+        r = ctx.reduce()
+        phi = ctx.get_phi()
+    g = spe.Grid(n, L, str(d["convention"]))
+    psi0 = d["psi0"]
+    v = spe.virial_terms(psi0, phi.astype(np.float64), g)
+    assert r["mass"] == pytest.approx(spe.mass(psi0, g), rel=1e-6)
+    rho = np.abs(psi0) ** 2
+    assert r["rho_max"] == pytest.approx(rho.max(), rel=1e-6)
+    assert int(r["argmax"]) == int(np.argmax(rho))
+    for key in ("VirialPotential", "TotalKineticE", "TotalQuantumE", "Virial"):
+        assert r[key] == pytest.approx(v[key], rel=1e-5, abs=1e-9)
+
+
+def test_cic_interpolation_matches_oracle(wdm):
+    n, L = (32, 32, 32), (8.0, 8.0, 8.0)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2)) + 0j).astype(np.complex64)
+    rng = np.random.default_rng(8)
+    pos = rng.uniform(-4.0, 4.0, size=(1000, 3))
+    with wdm.SPEContext(n, L, poisson_coeff=1.0) as ctx:
+        ctx.set_psi(psi0)
+        got = ctx.interpolate_phi(pos)
+        phi = ctx.get_phi().astype(np.float64)
+    ref = spe.cic_interpolate(g, phi, pos)
+    assert np.abs(got - ref).max() < 1e-5 * np.abs(ref).max()
+
+
+def test_nonfinite_is_reported(wdm):
+    from wavedm_gb300._abi import WdmError
+
+    n, L = (16, 16, 16), (4.0, 4.0, 4.0)
+    psi0 = np.ones((16, 16, 16), np.complex64)
+    psi0[3, 4, 5] = np.nan
+    with wdm.SPEContext(n, L) as ctx:
+        ctx.set_psi(psi0)
+        with pytest.raises(WdmError) as ei:
+            ctx.step(1, 0.01)
+        assert ei.value.status == 5
+        assert not ctx.is_finite()

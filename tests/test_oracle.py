@@ -1,0 +1,189 @@
+"""Pins of the FP64 oracle against the reference's own known answers and analytic cases.
+
+The reference stores no golden vectors; its tests pin the path by formulas and
+bounds, which are restated here:
+
+* grid spacing and cell volume            test/unit_test.jl:1-24
+* Poisson on a 32^3 Gaussian, loose bounds test/test_parallel.jl:70-97
+* harmonic oscillator exp(-x^2/2)exp(-it/2) test/simulation_SPE1D.jl:8-10,197-212
+* sech soliton A sech(A x/2) with a Kerr term test/simulation_SPE1D.jl:12-18,214-229
+  (the reference's phase omega = A^2/2 is not a solution of its own equation;
+  the self-consistent kappa = -(A/2)^2/A^2 and phase are used)
+* relative L2 metric                       test/simulation_SPE3D_validation.jl:85-88
+* drift factor of setup_fft_operators      src/solver/fft_operators.jl:8-15
+"""
+import numpy as np
+import pytest
+
+from oracle import spe
+
+
+def test_setup_grid_matches_reference_unit_test():
+    x, y, z, d, vol = spe.setup_grid(2.0, 2.0, 2.0, 64, 64, 64)
+    assert np.isclose(x.min(), -2.0) and np.isclose(x.max(), 2.0)
+    assert len(x) == len(y) == len(z) == 64
+    assert np.allclose(d, 4.0 / 63)
+    assert np.isclose(vol, np.prod(d))
+    x8, _, _, d8, _ = spe.setup_grid(1.0, 1.0, 1.0, 8, 8, 8)
+    assert len(x8) == 8 and np.isclose(d8[0], 2.0 / 7)
+    g = spe.Grid((64, 64, 64), (4.0, 4.0, 4.0), "reference")
+    assert np.allclose(g.spacing, 4.0 / 63)
+
+
+def test_rel_l2_definition():
+    a = np.array([1.0 + 1j, 2.0, 3.0])
+    b = np.array([1.0, 2.0, 3.0 + 0.5j])
+    ref = np.sqrt(np.mean(np.abs(a - b) ** 2)) / np.sqrt(np.mean(np.abs(b) ** 2))
+    assert spe.rel_l2(a, b) == pytest.approx(ref)
+
+
+def test_poisson_single_mode_exact():
+    n, L = (16, 12, 8), (2.0, 3.0, 1.5)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    k = 2 * np.pi * np.array([2 / L[0], 1 / L[1], 3 / L[2]])
+    rho = np.cos(k[0] * X + k[1] * Y + k[2] * Z) * np.ones((n[2], n[1], n[0]))
+    phi = spe.poisson(rho, g, coeff=4 * np.pi)
+    expect = -4 * np.pi * rho / np.dot(k, k)
+    assert np.abs(phi - expect).max() < 1e-12
+
+
+def test_poisson_gaussian_bounds_of_reference_test():
+    # test/test_parallel.jl:70-97: 32^3 Gaussian on LinRange(-pi, pi, 32), Delta = 1
+    x = np.linspace(-np.pi, np.pi, 32)
+    rho = np.exp(-(x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2))
+    g = spe.Grid((32, 32, 32), (32.0, 32.0, 32.0))  # spacing 1
+    phi = spe.poisson(rho, g, coeff=1.0)
+    assert np.all(np.isfinite(phi))
+    assert 1e-6 < np.abs(phi).max() < 100.0
+
+
+def test_drift_factor_matches_setup_fft_operators():
+    X, N, dt = 5.0, 16, 0.013
+    dense = spe.setup_fft_operators(X, X, X, N, N, N, dt)
+    g = spe.Grid((N, N, N), (2 * X, 2 * X, 2 * X), "reference")
+    assert np.abs(dense - np.exp(-0.5j * dt * g.k2())).max() < 1e-12
+
+
+def _line_grid(nx, L):
+    return spe.Grid((nx, 4, 4), (L, 1.0, 1.0))
+
+
+def _harmonic(dt, tmax, nx=64, L=20.0):
+    g = _line_grid(nx, L)
+    X, _, _ = g.coords()
+    psi0 = np.exp(-X ** 2 / 2) * np.ones((4, 4, nx))
+    phys = spe.Physics(poisson_coeff=0.0, tidal=lambda t: (1.0, 0, 0, 0, 0, 0))
+    nst = int(round(tmax / dt))
+    psi = spe.run(psi0, g, phys, dt, nst)
+    exact = psi0 * np.exp(-0.5j * nst * dt)
+    return spe.rel_l2(psi, exact)
+
+
+def test_harmonic_oscillator_ground_state():
+    assert _harmonic(0.01, 1.0) < 1e-4
+
+
+def test_strang_is_second_order():
+    e1 = _harmonic(0.1, 2.0)
+    e2 = _harmonic(0.05, 2.0)
+    assert 3.5 < e1 / e2 < 4.5
+
+
+def test_kerr_soliton_travels():
+    A, v = np.sqrt(2.0), 0.5
+    B = A / 2
+    kappa = -(B ** 2) / A ** 2
+    nx, L = 256, 60.0
+    g = _line_grid(nx, L)
+    X, _, _ = g.coords()
+
+    def sol(t):
+        return (A / np.cosh(B * (X - v * t)) * np.exp(1j * (v * X - 0.5 * (v * v - B * B) * t))) * np.ones((4, 4, nx))
+
+    phys = spe.Physics(poisson_coeff=0.0, kerr=kappa)
+    dt, nst = 0.005, 400
+    psi = spe.run(sol(0.0), g, phys, dt, nst)
+    assert spe.rel_l2(psi, sol(nst * dt)) < 1e-4
+
+
+def test_free_gaussian_dispersion():
+    s2, nx, L, t = 1.0, 256, 80.0, 3.0
+    g = _line_grid(nx, L)
+    X, _, _ = g.coords()
+    psi0 = np.exp(-X ** 2 / (2 * s2)) * np.ones((4, 4, nx))
+    exact = np.sqrt(s2 / (s2 + 1j * t)) * np.exp(-X ** 2 / (2 * (s2 + 1j * t))) * np.ones((4, 4, nx))
+    assert spe.rel_l2(spe.drift(psi0, g, t), exact) < 1e-10
+
+
+def _random_state(n, L, seed=1):
+    rng = np.random.default_rng(seed)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    r2 = X ** 2 + Y ** 2 + Z ** 2
+    psi = np.exp(-r2 / 4) * np.exp(1j * 0.3 * rng.standard_normal((n[2], n[1], n[0])))
+    return g, psi
+
+
+def test_strang_conserves_mass_and_is_time_reversible():
+    g, psi0 = _random_state((16, 16, 16), (8.0, 8.0, 8.0))
+    phys = spe.Physics(poisson_coeff=1.0, kerr=0.1,
+                       tidal=lambda t: (0.01 + 0.001 * t, -0.005, -0.005, 0.002, 0.0, 0.0))
+    dt = 0.02
+    psi = spe.run(psi0, g, phys, dt, 6)
+    assert abs(spe.mass(psi, g) / spe.mass(psi0, g) - 1) < 1e-12
+    back = spe.run(psi, g, phys, -dt, 6, t0=6 * dt)
+    assert spe.rel_l2(back, psi0) < 1e-12
+
+
+def test_reference_loop_is_half_kick_then_drift():
+    g, psi0 = _random_state((8, 8, 8), (6.0, 6.0, 6.0))
+    phys = spe.Physics(poisson_coeff=2.0)
+    dt = 0.05
+    one = spe.kdk_step(psi0, g, phys, 0.0, dt, mode="reference_loop")
+    manual = spe.drift(spe.kick(psi0, spe.potential(psi0, g, phys, 0.0), dt / 2), g, dt)
+    assert spe.rel_l2(one, manual) < 1e-14
+    lie = spe.kdk_step(psi0, g, phys, 0.0, dt, mode="lie")
+    manual = spe.drift(spe.kick(psi0, spe.potential(psi0, g, phys, 0.0), dt), g, dt)
+    assert spe.rel_l2(lie, manual) < 1e-14
+
+
+def test_absorbing_mask_values():
+    g = spe.Grid((16, 16, 16), (10.0, 10.0, 10.0), "reference")
+    m = spe.absorption_mask(g, alpha=10.0, dt=0.01)
+    assert np.all(m > 0) and np.all(m <= 1.0 + 1e-15)
+    # centre ~ 1; a face centre (x = X, y = z = 0) ~ exp(-alpha dt)
+    c = 8
+    assert m[c, c, c] == pytest.approx(1.0, abs=0.05)
+    assert m[c, c, -1] == pytest.approx(np.exp(-0.1), rel=1e-6)
+
+
+def test_cic_deposit_and_interpolation():
+    g = spe.Grid((16, 16, 16), (4.0, 4.0, 4.0))
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(-2.0, 2.0, size=(500, 3))
+    m = rng.uniform(0.5, 1.5, size=500)
+    rho = spe.cic_deposit(g, pos, m)
+    assert np.sum(rho) * g.dV == pytest.approx(m.sum(), rel=1e-12)
+    X, Y, Z = g.coords()
+    f = (0.3 * X + 0.2 * Y - 0.1 * Z) * np.ones((16, 16, 16))
+    inside = np.all((pos > -2.0) & (pos < 2.0 - 0.25), axis=1)
+    val = spe.cic_interpolate(g, f, pos[inside])
+    exact = pos[inside] @ np.array([0.3, 0.2, -0.1])
+    assert np.abs(val - exact).max() < 1e-12
+
+
+def test_virial_terms_plane_wave():
+    n, L = (16, 16, 16), (8.0, 8.0, 8.0)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    kx = 2 * np.pi * 2 / L[0]
+    psi = np.exp(1j * kx * X) * np.ones((16, 16, 16))
+    phi = np.zeros((16, 16, 16))
+    v = spe.virial_terms(psi, phi, g)
+    dx = g.spacing[0]
+    j = np.sin(kx * dx) / dx
+    nint = 14 ** 3
+    assert v["TotalKineticE"] == pytest.approx(0.5 * j * j * nint * g.dV, rel=1e-12)
+    assert abs(v["TotalQuantumE"]) < 1e-20
+    assert v["MomentumX"] == pytest.approx(j * nint * g.dV, rel=1e-12)

@@ -1,0 +1,213 @@
+"""Host-side handle on one libwavedm context (one grid size, `batch` halos).
+
+Arrays may be numpy arrays (host memory; copied through the C ABI's host
+path) or CUDA tensors exposing ``data_ptr()`` and ``is_cuda`` (device memory;
+used in place).  Layout is C order [batch][nz][ny][nx].
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import DEVICE, HOST, check
+
+
+def _is_device(a):
+    return getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if _is_device(a):
+        return C.c_void_p(a.data_ptr()), DEVICE
+    if not isinstance(a, np.ndarray):
+        raise TypeError(f"expected a numpy array or a CUDA tensor, got {type(a)!r}")
+    if not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous ([nz][ny][nx], x fastest)")
+    return C.c_void_p(a.ctypes.data), HOST
+
+
+class SPEContext:
+    """A device-resident Schroedinger-Poisson state and its fused KDK pipeline.
+
+    Parameters mirror ``wdm_desc``: grid points ``n=(nx, ny, nz)``, box
+    lengths ``L=(Lx, Ly, Lz)``, grid ``convention`` ("periodic" or
+    "reference"), ``poisson_coeff`` (4 pi G), ``kerr`` (kappa of kappa|psi|^2),
+    ``absorb_alpha`` (tanh mask), ``phase_mode`` ("plain" or "precise") and
+    ``batch`` (independent halos of this size).
+    """
+
+    def __init__(self, n, L, convention="periodic", poisson_coeff=1.0, kerr=0.0, absorb_alpha=0.0,
+                 phase_mode="precise", batch=1):
+        self.lib = _abi.load()
+        nx, ny, nz = (int(v) for v in n)
+        lx, ly, lz = (float(v) for v in L)
+        self.n = (nx, ny, nz)
+        self.L = (lx, ly, lz)
+        self.batch = int(batch)
+        self.shape = (nz, ny, nx) if self.batch == 1 else (self.batch, nz, ny, nx)
+        d = _abi.WdmDesc(nx, ny, nz, lx, ly, lz, _abi.CONVENTIONS[convention], float(poisson_coeff),
+                         float(kerr), float(absorb_alpha), _abi.PHASE_MODES[phase_mode], self.batch)
+        h = C.c_void_p()
+        check(self.lib.wdm_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    # lifecycle -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.wdm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise RuntimeError("context is closed")
+        return self._h
+
+    def _check(self, st):
+        return check(st, self.handle)
+
+    # state -----------------------------------------------------------------
+    def set_psi(self, psi):
+        if not _is_device(psi):
+            psi = np.ascontiguousarray(psi, dtype=np.complex64)
+            if psi.size != int(np.prod(self.shape)):
+                raise ValueError(f"psi has {psi.size} elements, the grid needs {int(np.prod(self.shape))}")
+        p, w = _ptr(psi)
+        self._check(self.lib.wdm_set_psi(self.handle, p, w))
+
+    def get_psi(self, out=None):
+        if out is None:
+            out = np.empty(self.shape, np.complex64)
+        p, w = _ptr(out)
+        self._check(self.lib.wdm_get_psi(self.handle, p, w))
+        return out
+
+    def get_rho(self, out=None):
+        if out is None:
+            out = np.empty(self.shape, np.float32)
+        p, w = _ptr(out)
+        self._check(self.lib.wdm_get_rho(self.handle, p, w))
+        return out
+
+    def get_phi(self, out=None):
+        if out is None:
+            out = np.empty(self.shape, np.float32)
+        p, w = _ptr(out)
+        self._check(self.lib.wdm_get_phi(self.handle, p, w))
+        return out
+
+    def set_static_potential(self, V):
+        if V is None:
+            self._check(self.lib.wdm_set_static_potential(self.handle, None, HOST))
+            return
+        if not _is_device(V):
+            V = np.ascontiguousarray(V, dtype=np.float32)
+        p, w = _ptr(V)
+        self._check(self.lib.wdm_set_static_potential(self.handle, p, w))
+
+    def set_tidal(self, schedule, per_item=False):
+        """Rows of (Txx, Tyy, Tzz, Txy, Txz, Tyz): row s is used by the s-th kick of the next step call."""
+        if schedule is None:
+            self._check(self.lib.wdm_set_tidal(self.handle, None, 0, 0))
+            return
+        s = np.ascontiguousarray(np.asarray(schedule, dtype=np.float64).reshape(-1, 6))
+        self._tidal_keep = s
+        self._check(self.lib.wdm_set_tidal(self.handle, C.c_void_p(s.ctypes.data), len(s), int(per_item)))
+
+    def set_particles(self, pos, mass):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        mass = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, np.float64), (len(pos),)))
+        self._check(self.lib.wdm_set_particles(self.handle, C.c_void_p(pos.ctypes.data),
+                                               C.c_void_p(mass.ctypes.data), len(pos)))
+
+    # the path ----------------------------------------------------------------
+    def step(self, nsteps, dt, t0=0.0, mode="strang", sync=True):
+        fn = self.lib.wdm_step if sync else self.lib.wdm_step_async
+        self._check(fn(self.handle, int(nsteps), float(dt), float(t0), _abi.STEP_MODES[mode]))
+
+    def kick(self, dt, t=0.0):
+        self._check(self.lib.wdm_kick(self.handle, float(dt), float(t)))
+
+    def drift(self, dt):
+        self._check(self.lib.wdm_drift(self.handle, float(dt)))
+
+    def poisson(self, rho, out=None):
+        if not _is_device(rho):
+            rho = np.ascontiguousarray(rho, dtype=np.float32)
+            if out is None:
+                out = np.empty(self.shape, np.float32)
+        pr, wr = _ptr(rho)
+        po, wo = _ptr(out)
+        if wr != wo:
+            raise ValueError("rho and phi must both be host or both be device arrays")
+        self._check(self.lib.wdm_poisson(self.handle, pr, po, wr))
+        return out
+
+    def fft3d(self, data_dev, inverse=False):
+        if not _is_device(data_dev):
+            raise TypeError("fft3d works in place on a CUDA tensor")
+        self._check(self.lib.wdm_fft3d(self.handle, C.c_void_p(data_dev.data_ptr()), 1 if inverse else -1))
+        return data_dev
+
+    # diagnostics ---------------------------------------------------------------
+    FIELDS = ("mass", "rho_max", "argmax", "com_x", "com_y", "com_z",
+              "VirialPotential", "TotalKineticE", "TotalQuantumE", "Virial")
+
+    def reduce(self):
+        out = np.zeros((self.batch, 10), np.float64)
+        self._check(self.lib.wdm_reduce(self.handle, C.c_void_p(out.ctypes.data)))
+        recs = [dict(zip(self.FIELDS, row.tolist())) for row in out]
+        return recs[0] if self.batch == 1 else recs
+
+    def interpolate_phi(self, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(pos), np.float64)
+        self._check(self.lib.wdm_interpolate_phi(self.handle, C.c_void_p(pos.ctypes.data), len(pos),
+                                                 C.c_void_p(out.ctypes.data)))
+        return out
+
+    def is_finite(self):
+        f = C.c_int32(0)
+        self._check(self.lib.wdm_check_finite(self.handle, C.byref(f)))
+        return bool(f.value)
+
+    @property
+    def stream(self):
+        return self.lib.wdm_stream(self.handle)
+
+    # profiling -------------------------------------------------------------------
+    def set_profiling(self, on=True):
+        self._check(self.lib.wdm_set_profiling(self.handle, int(bool(on))))
+
+    def profile(self):
+        """{pass name: dict(launches, ms, bytes_per_launch)} since profiling was turned on."""
+        n = self.lib.wdm_num_passes()
+        la = np.zeros(n, np.int64)
+        ms = np.zeros(n, np.float64)
+        by = np.zeros(n, np.float64)
+        self._check(self.lib.wdm_get_profile(self.handle, C.c_void_p(la.ctypes.data), C.c_void_p(ms.ctypes.data),
+                                             C.c_void_p(by.ctypes.data)))
+        return {self.lib.wdm_pass_name(p).decode(): dict(launches=int(la[p]), ms=float(ms[p]),
+                                                          bytes_per_launch=float(by[p])) for p in range(n)}
+
+    @property
+    def launch_count(self):
+        return int(self.lib.wdm_launch_count(self.handle))
+
+
+def size_supported(n):
+    return bool(_abi.load().wdm_size_supported(int(n)))

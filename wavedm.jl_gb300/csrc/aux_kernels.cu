@@ -1,0 +1,181 @@
+// Auxiliary kernels: density output, FP64 diagnostics reductions, CIC.
+#include "aux_kernels.cuh"
+
+namespace wdm {
+
+__global__ void k_abs2(const float2* __restrict__ psi, float* __restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 v = psi[i];
+    out[i] = v.x * v.x + v.y * v.y;
+  }
+}
+
+cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t st) {
+  const int blocks = (int)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16);
+  k_abs2<<<blocks, 256, 0, st>>>(psi, out, n);
+  return cudaGetLastError();
+}
+
+// One block partial per (block, batch item): RED_FIELDS doubles.  The sums
+// restate src/visualization/runtime.jl:210-238 (interior cells, second-order
+// central differences) and src/simulation_main.jl:652 (total mass).
+constexpr int RED_THREADS = 256;
+
+__global__ void __launch_bounds__(RED_THREADS)
+k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, RedGeom g,
+         double* __restrict__ partials) {
+  const long long nxy = (long long)g.nx * g.ny;
+  const long long n = nxy * g.nz;
+  const float2* psi = psi_all + blockIdx.y * n;
+  const float* phi = phi_all + blockIdx.y * n;
+  double acc[RED_FIELDS];
+#pragma unroll
+  for (int q = 0; q < RED_FIELDS; ++q) acc[q] = 0.0;
+  acc[RED_MAX] = -1.0;
+  acc[RED_ARG] = 0.0;
+  const double i2dx = 0.5 / g.dx, i2dy = 0.5 / g.dy, i2dz = 0.5 / g.dz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / nxy);
+    const long long rem = i - z * nxy;
+    const int y = (int)(rem / g.nx);
+    const int x = (int)(rem - (long long)y * g.nx);
+    const float2 p = psi[i];
+    const double rho = (double)p.x * p.x + (double)p.y * p.y;
+    acc[RED_MASS] += rho;
+    acc[RED_MX] += rho * (g.x0 + g.dx * x);
+    acc[RED_MY] += rho * (g.y0 + g.dy * y);
+    acc[RED_MZ] += rho * (g.z0 + g.dz * z);
+    if (rho > acc[RED_MAX]) {
+      acc[RED_MAX] = rho;
+      acc[RED_ARG] = (double)i;
+    }
+    if (x > 0 && x < g.nx - 1 && y > 0 && y < g.ny - 1 && z > 0 && z < g.nz - 1) {
+      acc[RED_W] += rho * (double)phi[i];
+      const float2 xp = psi[i + 1], xm = psi[i - 1];
+      const float2 yp = psi[i + g.nx], ym = psi[i - g.nx];
+      const float2 zp = psi[i + nxy], zm = psi[i - nxy];
+      // rho v = Im(conj(psi) grad psi)
+      const double gxr = (xp.x - xm.x) * i2dx, gxi = (xp.y - xm.y) * i2dx;
+      const double gyr = (yp.x - ym.x) * i2dy, gyi = (yp.y - ym.y) * i2dy;
+      const double gzr = (zp.x - zm.x) * i2dz, gzi = (zp.y - zm.y) * i2dz;
+      const double jx = p.x * gxi - p.y * gxr;
+      const double jy = p.x * gyi - p.y * gyr;
+      const double jz = p.x * gzi - p.y * gzr;
+      if (rho > 0) acc[RED_K] += (jx * jx + jy * jy + jz * jz) / rho;
+      const double ax = (sqrt((double)xp.x * xp.x + (double)xp.y * xp.y) - sqrt((double)xm.x * xm.x + (double)xm.y * xm.y)) * i2dx;
+      const double ay = (sqrt((double)yp.x * yp.x + (double)yp.y * yp.y) - sqrt((double)ym.x * ym.x + (double)ym.y * ym.y)) * i2dy;
+      const double az = (sqrt((double)zp.x * zp.x + (double)zp.y * zp.y) - sqrt((double)zm.x * zm.x + (double)zm.y * zm.y)) * i2dz;
+      acc[RED_Q] += ax * ax + ay * ay + az * az;
+    }
+  }
+  // block reduction (warp shuffles, then one warp over the warp results)
+  __shared__ double sh[RED_THREADS / 32][RED_FIELDS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int q = 0; q < RED_FIELDS; ++q) {
+      const double o = __shfl_down_sync(0xffffffffu, acc[q], off);
+      if (q == RED_MAX || q == RED_ARG) continue;
+      acc[q] += o;
+    }
+    const double om = __shfl_down_sync(0xffffffffu, acc[RED_MAX], off);
+    const double oa = __shfl_down_sync(0xffffffffu, acc[RED_ARG], off);
+    if (om > acc[RED_MAX] || (om == acc[RED_MAX] && oa < acc[RED_ARG])) {
+      acc[RED_MAX] = om;
+      acc[RED_ARG] = oa;
+    }
+  }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < RED_FIELDS; ++q) sh[w][q] = acc[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r[RED_FIELDS];
+#pragma unroll
+    for (int q = 0; q < RED_FIELDS; ++q) r[q] = sh[0][q];
+    for (int k = 1; k < RED_THREADS / 32; ++k) {
+      for (int q = 0; q < RED_FIELDS; ++q)
+        if (q != RED_MAX && q != RED_ARG) r[q] += sh[k][q];
+      if (sh[k][RED_MAX] > r[RED_MAX] || (sh[k][RED_MAX] == r[RED_MAX] && sh[k][RED_ARG] < r[RED_ARG])) {
+        r[RED_MAX] = sh[k][RED_MAX];
+        r[RED_ARG] = sh[k][RED_ARG];
+      }
+    }
+    double* o = partials + ((long long)blockIdx.y * gridDim.x + blockIdx.x) * RED_FIELDS;
+    for (int q = 0; q < RED_FIELDS; ++q) o[q] = r[q];
+  }
+}
+
+cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g, double* partials, int nblocks,
+                          int batch, cudaStream_t st) {
+  k_reduce<<<dim3(nblocks, batch), RED_THREADS, 0, st>>>(psi, phi, g, partials);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ long long cic_cell(int ix, int iy, int iz, int nx, int ny, int nz) {
+  ix = ix >= nx ? ix - nx : ix;
+  iy = iy >= ny ? iy - ny : iy;
+  iz = iz >= nz ? iz - nz : iz;
+  return ((long long)iz * ny + iy) * nx + ix;
+}
+
+__global__ void k_cic_deposit(float* __restrict__ rho, const CicParticle* __restrict__ p, long long n, int nx, int ny,
+                              int nz) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const CicParticle a = p[q];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ox = c & 1, oy = (c >> 1) & 1, oz = c >> 2;
+    const float w = (ox ? a.f[0] : 1.f - a.f[0]) * (oy ? a.f[1] : 1.f - a.f[1]) * (oz ? a.f[2] : 1.f - a.f[2]);
+    atomicAdd(rho + cic_cell(a.i[0] + ox, a.i[1] + oy, a.i[2] + oz, nx, ny, nz), a.m * w);
+  }
+}
+
+__global__ void k_cic_clear(float* __restrict__ rho, const CicParticle* __restrict__ p, long long n, int nx, int ny,
+                            int nz) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const CicParticle a = p[q];
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    rho[cic_cell(a.i[0] + (c & 1), a.i[1] + ((c >> 1) & 1), a.i[2] + (c >> 2), nx, ny, nz)] = 0.f;
+}
+
+__global__ void k_cic_interp(const float* __restrict__ f, const CicParticle* __restrict__ p, long long n, int nx,
+                             int ny, int nz, double* __restrict__ out) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const CicParticle a = p[q];
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ox = c & 1, oy = (c >> 1) & 1, oz = c >> 2;
+    const double w = (double)(ox ? a.f[0] : 1.f - a.f[0]) * (oy ? a.f[1] : 1.f - a.f[1]) * (oz ? a.f[2] : 1.f - a.f[2]);
+    s += w * f[cic_cell(a.i[0] + ox, a.i[1] + oy, a.i[2] + oz, nx, ny, nz)];
+  }
+  out[q] = s;
+}
+
+cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz,
+                               cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_cic_deposit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cic_clear(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_cic_clear<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cic_interp(const float* field, const CicParticle* p, long long n, int nx, int ny, int nz,
+                              double* out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_cic_interp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(field, p, n, nx, ny, nz, out);
+  return cudaGetLastError();
+}
+
+}  // namespace wdm

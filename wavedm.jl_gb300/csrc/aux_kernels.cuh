@@ -1,0 +1,43 @@
+// Auxiliary kernels: density output, FP64 diagnostics reductions, CIC.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace wdm {
+
+// CIC particle: base cell (wrapped into the grid) and fractional offsets in
+// [0, 1) along each axis, built in FP64 on the host; m = mass / dV.
+struct CicParticle {
+  int i[3];
+  float f[3];
+  float m;
+};
+
+enum {
+  RED_MASS = 0,  // sum rho
+  RED_MAX,       // max rho
+  RED_ARG,       // flat index of the max
+  RED_MX,        // sum rho x
+  RED_MY,
+  RED_MZ,
+  RED_W,         // sum rho Phi over interior cells
+  RED_K,         // sum (rho v)^2 / rho over interior cells
+  RED_Q,         // sum |grad sqrt rho|^2 over interior cells
+  RED_FIELDS
+};
+
+struct RedGeom {
+  int nx, ny, nz;
+  double dx, dy, dz, x0, y0, z0;
+};
+
+cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t st);
+cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g, double* partials, int nblocks,
+                          int batch, cudaStream_t st);
+cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz,
+                               cudaStream_t st);
+cudaError_t launch_cic_clear(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, cudaStream_t st);
+cudaError_t launch_cic_interp(const float* field, const CicParticle* p, long long n, int nx, int ny, int nz,
+                              double* out, cudaStream_t st);
+
+}  // namespace wdm

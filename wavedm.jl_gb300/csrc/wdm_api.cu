@@ -1,0 +1,963 @@
+// C-ABI of libwavedm: context, tables, step orchestration, diagnostics, CIC.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/wavedm.h"
+#include "aux_kernels.cuh"
+#include "kernel_set.h"
+
+namespace wdm {
+const KernelSet* ks_8();
+const KernelSet* ks_12();
+const KernelSet* ks_16();
+const KernelSet* ks_24();
+const KernelSet* ks_32();
+const KernelSet* ks_48();
+const KernelSet* ks_64();
+const KernelSet* ks_96();
+const KernelSet* ks_128();
+const KernelSet* ks_192();
+const KernelSet* ks_256();
+const KernelSet* ks_384();
+const KernelSet* ks_512();
+
+const KernelSet* kernels_for(int n) {
+  switch (n) {
+    case 8: return ks_8();
+    case 12: return ks_12();
+    case 16: return ks_16();
+    case 24: return ks_24();
+    case 32: return ks_32();
+    case 48: return ks_48();
+    case 64: return ks_64();
+    case 96: return ks_96();
+    case 128: return ks_128();
+    case 192: return ks_192();
+    case 256: return ks_256();
+    case 384: return ks_384();
+    case 512: return ks_512();
+    default: return nullptr;
+  }
+}
+}  // namespace wdm
+
+using namespace wdm;
+
+static std::string g_create_error;
+
+// Passes of the pipeline, for launch counting and per-pass event timing.
+enum Pass {
+  P_KICK_FWD = 0,  // P1: Phi C2R + kick + psi x-FFT
+  P_PSI_Y_FWD,     // P2
+  P_PSI_Z_DRIFT,   // P3
+  P_PSI_Y_INV,     // P4
+  P_X_INV_RHO,     // P5: psi x-iFFT (+mask) + density R2C
+  P_H_Y_FWD,       // P6
+  P_H_Z_POISSON,   // P7
+  P_H_Y_INV,       // P8
+  P_KICK,          // final half kick (no FFT)
+  P_DENSITY,       // density R2C of real-space psi (start of a run)
+  P_CIC_DEPOSIT,
+  P_CIC_CLEAR,
+  P_X_FFT,         // plain x-FFT (wdm_drift)
+  P_PHI_OUT,       // Phi C2R to a real field
+  NPASS
+};
+static const char* const PASS_NAMES[NPASS] = {
+    "kick_xfft_fwd", "psi_y_fwd", "psi_z_drift", "psi_y_inv", "psi_x_inv_rho", "rho_y_fwd", "rho_z_poisson",
+    "phi_y_inv",     "kick_final", "rho_density", "cic_deposit", "cic_clear", "psi_x_fwd", "phi_x_c2r"};
+
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  struct Rec {
+    int pass;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> pending;
+  int64_t launches[NPASS] = {0};
+  double ms[NPASS] = {0};
+};
+
+struct wdm_ctx {
+  wdm_desc d{};
+  int nxh = 0;
+  long long ncell = 0;   // cells per batch item
+  long long nhalf = 0;   // half-spectrum entries per batch item
+  cudaStream_t st = nullptr;
+  const KernelSet *kx = nullptr, *ky = nullptr, *kz = nullptr;
+  double dx = 0, dy = 0, dz = 0, x0 = 0, y0 = 0, z0 = 0;
+  // device buffers
+  float2* psi = nullptr;
+  float2* H = nullptr;
+  float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  float *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
+  float2 *cx = nullptr, *cy = nullptr, *cz = nullptr;  // precise drift tables (cached per dt)
+  double tab_dt = NAN;
+  float *mx = nullptr, *my = nullptr, *mz = nullptr;     // absorbing mask tables (cached per dt)
+  double mask_dt = NAN;
+  float* V = nullptr;
+  float* rho_b = nullptr;
+  CicParticle* parts = nullptr;
+  long long nparts = 0;
+  float* T6b = nullptr;             // per-batch-item tidal tensors
+  std::vector<double> tide;         // host schedule rows of 6
+  int tide_on = 0;
+  int* flag = nullptr;              // device non-finite flag
+  float* scratch_f = nullptr;       // float field scratch [batch][ncell]
+  float2* scratch_h = nullptr;      // half-spectrum scratch
+  double* red = nullptr;            // reduction partials
+  int red_blocks = 0;
+  int have_psi = 0;
+  int phi_valid = 0;
+  int64_t launch_count = 0;
+  Profiler prof;
+  std::string err;
+};
+
+static cudaEvent_t prof_event(wdm_ctx* c) {
+  if (!c->prof.pool.empty()) {
+    cudaEvent_t e = c->prof.pool.back();
+    c->prof.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Collect finished event pairs into the per-pass totals.
+static cudaError_t prof_flush(wdm_ctx* c) {
+  if (c->prof.pending.empty()) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return e;
+  for (auto& r : c->prof.pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) c->prof.ms[r.pass] += ms;
+    c->prof.launches[r.pass] += 1;
+    c->prof.pool.push_back(r.a);
+    c->prof.pool.push_back(r.b);
+  }
+  c->prof.pending.clear();
+  return cudaSuccess;
+}
+
+// Run one pass launch: counted always, bracketed by events when profiling.
+template <class F>
+static cudaError_t run_pass(wdm_ctx* c, int pass, F launch) {
+  c->launch_count += 1;
+  if (!c->prof.on) return launch();
+  cudaEvent_t a = prof_event(c), b = prof_event(c);
+  cudaEventRecord(a, c->st);
+  cudaError_t e = launch();
+  cudaEventRecord(b, c->st);
+  c->prof.pending.push_back({pass, a, b});
+  if (c->prof.pending.size() > 4096) {
+    cudaError_t f = prof_flush(c);
+    if (e == cudaSuccess) e = f;
+  }
+  return e;
+}
+
+// Algorithmic bytes of one launch of a pass: every operand read once and
+// written once (complex64 8 B, float 4 B), all batch items.
+static double pass_bytes(const wdm_ctx* c, int p) {
+  const double B = c->d.batch, nc = (double)c->ncell * B, nh = (double)c->nhalf * B;
+  switch (p) {
+    case P_KICK_FWD:
+    case P_KICK: return 16.0 * nc + 8.0 * nh + (c->V ? 4.0 * nc : 0.0);
+    case P_PSI_Y_FWD:
+    case P_PSI_Z_DRIFT:
+    case P_PSI_Y_INV:
+    case P_X_FFT: return 16.0 * nc;
+    case P_X_INV_RHO: return 16.0 * nc + 8.0 * nh + (c->nparts ? 4.0 * c->ncell : 0.0);
+    case P_DENSITY: return 8.0 * nc + 8.0 * nh + (c->nparts ? 4.0 * c->ncell : 0.0);
+    case P_H_Y_FWD:
+    case P_H_Z_POISSON:
+    case P_H_Y_INV: return 16.0 * nh;
+    case P_CIC_DEPOSIT: return (double)c->nparts * (sizeof(CicParticle) + 8 * 2 * sizeof(float));
+    case P_CIC_CLEAR: return (double)c->nparts * (sizeof(CicParticle) + 8 * sizeof(float));
+    case P_PHI_OUT: return 8.0 * nh + 4.0 * nc;
+    default: return 0.0;
+  }
+}
+
+// --------------------------------------------------------------------------
+// helpers
+// --------------------------------------------------------------------------
+static wdm_status fail(wdm_ctx* c, wdm_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_error = msg;
+  return s;
+}
+
+static wdm_status cuda_fail(wdm_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, WDM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define WDM_CU(c, call)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail((c), e_, #call); \
+  } while (0)
+
+static bool fault_injected(const char* what) {
+  const char* f = std::getenv("WDM_FAULT");
+  return f && std::strstr(f, what) != nullptr;
+}
+
+template <class T>
+static wdm_status dalloc(wdm_ctx* c, T** p, size_t count) {
+  if (fault_injected("alloc")) return fail(c, WDM_ERR_ALLOC, "injected allocation failure (WDM_FAULT=alloc)");
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T) + 16);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(c, WDM_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return WDM_OK;
+}
+
+#define WDM_TRY(x)                    \
+  do {                                \
+    wdm_status s_ = (x);              \
+    if (s_ != WDM_OK) return s_;      \
+  } while (0)
+
+static void axis_geom(int n, double L, int conv, double* d, double* x0) {
+  if (conv == WDM_GRID_REFERENCE) {
+    *d = L / (n - 1);
+    *x0 = -L / 2;
+  } else {
+    *d = L / n;
+    *x0 = -L / 2;
+  }
+}
+
+// angular wavenumber of FFT index m on an axis of n points and period L
+static double kval(int m, int n, double L) {
+  const int s = (m < (n + 1) / 2) ? m : m - n;  // fftfreq order: 0..ceil(n/2)-1, -floor(n/2)..-1
+  return 2.0 * M_PI * s / L;
+}
+
+static wdm_status upload_twiddles(wdm_ctx* c, float2** dst, int n) {
+  std::vector<float2> h(n);
+  for (int m = 0; m < n; ++m) {
+    const double a = -2.0 * M_PI * (double)m / (double)n;
+    h[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  WDM_TRY(dalloc(c, dst, n));
+  WDM_CU(c, cudaMemcpy(*dst, h.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
+  return WDM_OK;
+}
+
+static wdm_status upload_k2(wdm_ctx* c, float** dst, int n, double L) {
+  std::vector<float> h(n);
+  for (int m = 0; m < n; ++m) {
+    const double k = kval(m, n, L);
+    h[m] = (float)(k * k);
+  }
+  WDM_TRY(dalloc(c, dst, n));
+  WDM_CU(c, cudaMemcpy(*dst, h.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  return WDM_OK;
+}
+
+// Drift phase tables exp(-i k_a^2 dt/2) built in FP64 (argument reduced mod 2pi
+// in double before cos/sin); the z table carries 1/(nx ny nz).
+static wdm_status ensure_drift_tables(wdm_ctx* c, double dt) {
+  if (c->tab_dt == dt) return WDM_OK;
+  const int n[3] = {c->d.nx, c->d.ny, c->d.nz};
+  const double L[3] = {c->d.lx, c->d.ly, c->d.lz};
+  float2* dst[3] = {c->cx, c->cy, c->cz};
+  const double scale = 1.0 / ((double)c->d.nx * c->d.ny * c->d.nz);
+  for (int a = 0; a < 3; ++a) {
+    std::vector<float2> h(n[a]);
+    for (int m = 0; m < n[a]; ++m) {
+      const double k = kval(m, n[a], L[a]);
+      const double th = std::fmod(0.5 * k * k * dt, 2.0 * M_PI);
+      const double s = (a == 2) ? scale : 1.0;
+      h[m] = make_float2((float)(s * std::cos(th)), (float)(-s * std::sin(th)));
+    }
+    WDM_CU(c, cudaMemcpyAsync(dst[a], h.data(), n[a] * sizeof(float2), cudaMemcpyHostToDevice, c->st));
+    WDM_CU(c, cudaStreamSynchronize(c->st));
+  }
+  c->tab_dt = dt;
+  return WDM_OK;
+}
+
+// Absorbing mask exp(-alpha dt (6 - tanh((x+X)/w) + tanh((x-X)/w) - ...)) of
+// src/solver/fft_operators.jl:22-27 factorises into one table per axis:
+// m_a(x) = exp(-alpha dt (2 - tanh((x+X)/w) + tanh((x-X)/w))), w = X/50.
+static wdm_status ensure_mask_tables(wdm_ctx* c, double dt) {
+  if (c->d.absorb_alpha == 0.0 || c->mask_dt == dt) return WDM_OK;
+  const int n[3] = {c->d.nx, c->d.ny, c->d.nz};
+  const double L[3] = {c->d.lx, c->d.ly, c->d.lz};
+  const double d[3] = {c->dx, c->dy, c->dz};
+  const double o[3] = {c->x0, c->y0, c->z0};
+  float* dst[3] = {c->mx, c->my, c->mz};
+  for (int a = 0; a < 3; ++a) {
+    const double X = L[a] / 2, w = X / 50;
+    std::vector<float> h(n[a]);
+    for (int i = 0; i < n[a]; ++i) {
+      const double x = o[a] + d[a] * i;
+      h[i] = (float)std::exp(-c->d.absorb_alpha * dt * (2.0 - std::tanh((x + X) / w) + std::tanh((x - X) / w)));
+    }
+    WDM_CU(c, cudaMemcpyAsync(dst[a], h.data(), n[a] * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    WDM_CU(c, cudaStreamSynchronize(c->st));
+  }
+  c->mask_dt = dt;
+  return WDM_OK;
+}
+
+static RowGeom rows_psi(const wdm_ctx* c) {
+  RowGeom r;
+  r.nrows = c->d.ny * c->d.nz;
+  r.ny = c->d.ny;
+  r.pitch = c->d.nx;
+  r.bstride = c->ncell;
+  return r;
+}
+
+static LineGeom lines_y(const wdm_ctx* c, int xext, long long bstride) {
+  LineGeom g;
+  g.nlines = xext * c->d.nz;
+  g.nxa = xext;
+  g.outer = (long long)c->d.ny * xext;
+  g.pstride = xext;
+  g.bstride = bstride;
+  return g;
+}
+
+static LineGeom lines_z(const wdm_ctx* c, int xext, long long bstride) {
+  LineGeom g;
+  g.nlines = xext * c->d.ny;
+  g.nxa = xext;
+  g.outer = xext;
+  g.pstride = (long long)c->d.ny * xext;
+  g.bstride = bstride;
+  return g;
+}
+
+// --------------------------------------------------------------------------
+// pipeline pieces
+// --------------------------------------------------------------------------
+// density (+baryons) of psi -> H, then the Poisson solve on H (P5..P8).
+// write_psi != 0: psi holds x-spectral data (after P4); the pass inverts it
+// first (with the absorbing mask) and writes real-space psi back.
+static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
+  const int B = c->d.batch;
+  if (c->nparts > 0) {
+    cudaError_t e = run_pass(c, P_CIC_DEPOSIT, [&] {
+      return launch_cic_deposit(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->st);
+    });
+    if (e != cudaSuccess) return cuda_fail(c, e, "cic deposit");
+  }
+  RhoArgs ra{};
+  const bool mask = write_psi && c->d.absorb_alpha != 0.0;
+  if (mask) WDM_TRY(ensure_mask_tables(c, dt_mask));
+  ra.mx = mask ? c->mx : nullptr;
+  ra.my = mask ? c->my : nullptr;
+  ra.mz = mask ? c->mz : nullptr;
+  ra.rho_b = c->nparts > 0 ? c->rho_b : nullptr;
+  ra.rb_bstride = 0;
+  ra.write_psi = write_psi;
+  ra.nonfinite = c->flag;
+  cudaError_t e = run_pass(c, write_psi ? P_X_INV_RHO : P_DENSITY, [&] {
+    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, ra, B, c->st);
+  });
+  if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
+  if (c->nparts > 0) {
+    e = run_pass(c, P_CIC_CLEAR, [&] {
+      return launch_cic_clear(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->st);
+    });
+    if (e != cudaSuccess) return cuda_fail(c, e, "cic clear");
+  }
+  if ((e = run_pass(c, P_H_Y_FWD, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st); })) !=
+      cudaSuccess)
+    return cuda_fail(c, e, "H y fwd");
+  PoissonOp po;
+  po.kx2 = c->kx2;
+  po.ky2 = c->ky2;
+  po.kz2 = c->kz2;
+  po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
+  po.nxa = c->nxh;
+  if ((e = run_pass(c, P_H_Z_POISSON,
+                    [&] { return c->kz->lfft_poisson(c->H, lines_z(c, c->nxh, c->nhalf), c->twz, po, B, c->st); })) !=
+      cudaSuccess)
+    return cuda_fail(c, e, "H z poisson");
+  if ((e = run_pass(c, P_H_Y_INV, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->nhalf), c->twy, true, B, c->st); })) !=
+      cudaSuccess)
+    return cuda_fail(c, e, "H y inv");
+  c->phi_valid = 1;
+  return WDM_OK;
+}
+
+static void split_dt(double dt, float* hi, float* lo) {
+  *hi = (float)dt;
+  *lo = (float)(dt - (double)*hi);
+}
+
+static KickArgs kick_args(const wdm_ctx* c, double dt, int sched_row) {
+  KickArgs a{};
+  split_dt(dt, &a.dt_hi, &a.dt_lo);
+  a.T6b = nullptr;
+  a.tidal = 0;
+  if (c->tide_on == 2) {
+    a.T6b = c->T6b;
+    a.tidal = 1;
+  } else if (c->tide_on == 1) {
+    const int nrow = (int)(c->tide.size() / 6);
+    const int r = sched_row < nrow ? sched_row : nrow - 1;
+    for (int q = 0; q < 6; ++q) a.T6[q] = (float)c->tide[6 * r + q];
+    a.tidal = 1;
+  }
+  a.x0 = (float)c->x0;
+  a.y0 = (float)c->y0;
+  a.z0 = (float)c->z0;
+  a.dx = (float)c->dx;
+  a.dy = (float)c->dy;
+  a.dz = (float)c->dz;
+  a.kerr = (float)c->d.kerr;
+  a.V = c->V;
+  a.v_bstride = c->ncell;
+  a.precise = c->d.phase_mode == WDM_PHASE_PRECISE;
+  return a;
+}
+
+static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd) {
+  KickArgs a = kick_args(c, dt, sched_row);
+  cudaError_t e = run_pass(c, fwd ? P_KICK_FWD : P_KICK, [&] {
+    return c->kx->x_kick(c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
+  });
+  if (e != cudaSuccess) return cuda_fail(c, e, "x_kick");
+  return WDM_OK;
+}
+
+// P2..P4 on x-spectral psi: y fwd, z fwd * drift phase * inverse, y inverse.
+static wdm_status drift_yz(wdm_ctx* c, double dt) {
+  const int B = c->d.batch;
+  DriftOp op{};
+  const bool precise = c->d.phase_mode == WDM_PHASE_PRECISE;
+  if (precise) WDM_TRY(ensure_drift_tables(c, dt));
+  op.cx = c->cx;
+  op.cy = c->cy;
+  op.cz = c->cz;
+  op.kx2 = c->kx2;
+  op.ky2 = c->ky2;
+  op.kz2 = c->kz2;
+  op.half_dt = (float)(0.5 * dt);
+  op.scale = (float)(1.0 / ((double)c->d.nx * c->d.ny * c->d.nz));
+  op.nxa = c->d.nx;
+  op.precise = precise;
+  op.tab_bstride = 0;
+  cudaError_t e;
+  if ((e = run_pass(c, P_PSI_Y_FWD,
+                    [&] { return c->ky->lfft(c->psi, lines_y(c, c->d.nx, c->ncell), c->twy, false, B, c->st); })) !=
+      cudaSuccess)
+    return cuda_fail(c, e, "psi y fwd");
+  if ((e = run_pass(c, P_PSI_Z_DRIFT,
+                    [&] { return c->kz->lfft_drift(c->psi, lines_z(c, c->d.nx, c->ncell), c->twz, op, B, c->st); })) !=
+      cudaSuccess)
+    return cuda_fail(c, e, "psi z drift");
+  if ((e = run_pass(c, P_PSI_Y_INV,
+                    [&] { return c->ky->lfft(c->psi, lines_y(c, c->d.nx, c->ncell), c->twy, true, B, c->st); })) !=
+      cudaSuccess)
+    return cuda_fail(c, e, "psi y inv");
+  return WDM_OK;
+}
+
+static wdm_status sync_and_check(wdm_ctx* c) {
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  int flag = 0;
+  WDM_CU(c, cudaMemcpy(&flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (fault_injected("nonfinite")) flag = 1;
+  if (flag) return fail(c, WDM_ERR_NONFINITE, "psi became non-finite (NaN/Inf density)");
+  return WDM_OK;
+}
+
+static wdm_status need_psi(wdm_ctx* c) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (!c->have_psi) return fail(c, WDM_ERR_STATE, "psi has not been set (call wdm_set_psi first)");
+  return WDM_OK;
+}
+
+static wdm_status copy_in(wdm_ctx* c, void* dst, const void* src, size_t bytes, int where) {
+  if (!src) return fail(c, WDM_ERR_INVALID, "null input pointer");
+  if (where != WDM_HOST && where != WDM_DEVICE) return fail(c, WDM_ERR_INVALID, "where must be WDM_HOST or WDM_DEVICE");
+  WDM_CU(c, cudaMemcpyAsync(dst, src, bytes, where == WDM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                            c->st));
+  return WDM_OK;
+}
+
+static wdm_status copy_out(wdm_ctx* c, void* dst, const void* src, size_t bytes, int where) {
+  if (!dst) return fail(c, WDM_ERR_INVALID, "null output pointer");
+  if (where != WDM_HOST && where != WDM_DEVICE) return fail(c, WDM_ERR_INVALID, "where must be WDM_HOST or WDM_DEVICE");
+  WDM_CU(c, cudaMemcpyAsync(dst, src, bytes, where == WDM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                            c->st));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  return WDM_OK;
+}
+
+static wdm_status ensure_scratch(wdm_ctx* c) {
+  if (!c->scratch_f) WDM_TRY(dalloc(c, &c->scratch_f, (size_t)c->ncell * c->d.batch));
+  if (!c->scratch_h) WDM_TRY(dalloc(c, &c->scratch_h, (size_t)c->nhalf * c->d.batch));
+  return WDM_OK;
+}
+
+// --------------------------------------------------------------------------
+// C ABI
+// --------------------------------------------------------------------------
+extern "C" {
+
+int32_t wdm_version(void) { return 1; }
+
+int32_t wdm_size_supported(int32_t n) { return kernels_for(n) != nullptr ? 1 : 0; }
+
+const char* wdm_last_error(const wdm_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+void* wdm_stream(wdm_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
+
+wdm_status wdm_destroy(wdm_ctx* c) {
+  if (!c) return WDM_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
+                  c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->parts, c->T6b, c->flag, c->scratch_f,
+                  c->scratch_h, c->red};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  for (auto& r : c->prof.pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return WDM_OK;
+}
+
+wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
+  if (!d || !out) return fail(nullptr, WDM_ERR_INVALID, "wdm_create: null argument");
+  *out = nullptr;
+  const int n[3] = {d->nx, d->ny, d->nz};
+  for (int a = 0; a < 3; ++a)
+    if (!kernels_for(n[a]))
+      return fail(nullptr, WDM_ERR_UNSUPPORTED,
+                  "wdm_create: axis length " + std::to_string(n[a]) +
+                      " has no FFT plan (supported: 8 12 16 24 32 48 64 96 128 192 256 384 512)");
+  if (!(d->lx > 0 && d->ly > 0 && d->lz > 0)) return fail(nullptr, WDM_ERR_INVALID, "wdm_create: box lengths must be > 0");
+  if (d->batch < 1) return fail(nullptr, WDM_ERR_INVALID, "wdm_create: batch must be >= 1");
+  if (d->convention != WDM_GRID_PERIODIC && d->convention != WDM_GRID_REFERENCE)
+    return fail(nullptr, WDM_ERR_INVALID, "wdm_create: unknown grid convention");
+  if (d->phase_mode != WDM_PHASE_PLAIN && d->phase_mode != WDM_PHASE_PRECISE)
+    return fail(nullptr, WDM_ERR_INVALID, "wdm_create: unknown phase mode");
+  const long long ncell = (long long)d->nx * d->ny * d->nz;
+  if (ncell * d->batch > (1LL << 31) - 1) return fail(nullptr, WDM_ERR_UNSUPPORTED, "wdm_create: batch*cells exceeds 2^31");
+  wdm_ctx* c = new wdm_ctx();
+  c->d = *d;
+  c->nxh = d->nx / 2 + 1;
+  c->ncell = ncell;
+  c->nhalf = (long long)c->nxh * d->ny * d->nz;
+  c->kx = kernels_for(d->nx);
+  c->ky = kernels_for(d->ny);
+  c->kz = kernels_for(d->nz);
+  axis_geom(d->nx, d->lx, d->convention, &c->dx, &c->x0);
+  axis_geom(d->ny, d->ly, d->convention, &c->dy, &c->y0);
+  axis_geom(d->nz, d->lz, d->convention, &c->dz, &c->z0);
+  wdm_status s = WDM_OK;
+  auto bail = [&](wdm_status st) {
+    g_create_error = c->err;
+    wdm_destroy(c);
+    return st;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cuda_fail(c, e, "cudaStreamCreate");
+    return bail(WDM_ERR_CUDA);
+  }
+  const size_t B = (size_t)d->batch;
+  if ((s = dalloc(c, &c->psi, B * ncell)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->H, B * c->nhalf)) != WDM_OK) return bail(s);
+  if ((s = upload_twiddles(c, &c->twx, d->nx)) != WDM_OK) return bail(s);
+  if ((s = upload_twiddles(c, &c->twy, d->ny)) != WDM_OK) return bail(s);
+  if ((s = upload_twiddles(c, &c->twz, d->nz)) != WDM_OK) return bail(s);
+  if ((s = upload_k2(c, &c->kx2, d->nx, d->lx)) != WDM_OK) return bail(s);
+  if ((s = upload_k2(c, &c->ky2, d->ny, d->ly)) != WDM_OK) return bail(s);
+  if ((s = upload_k2(c, &c->kz2, d->nz, d->lz)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->cx, d->nx)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->cy, d->ny)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->cz, d->nz)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->mx, d->nx)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->my, d->ny)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->mz, d->nz)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->flag, 1)) != WDM_OK) return bail(s);
+  if ((e = cudaMemsetAsync(c->flag, 0, sizeof(int), c->st)) != cudaSuccess) {
+    cuda_fail(c, e, "memset flag");
+    return bail(WDM_ERR_CUDA);
+  }
+  c->red_blocks = 4 * 152;
+  if ((s = dalloc(c, &c->red, B * c->red_blocks * RED_FIELDS)) != WDM_OK) return bail(s);
+  if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) {
+    cuda_fail(c, e, "sync");
+    return bail(WDM_ERR_CUDA);
+  }
+  *out = c;
+  return WDM_OK;
+}
+
+wdm_status wdm_set_psi(wdm_ctx* c, const void* psi, int32_t where) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  WDM_TRY(copy_in(c, c->psi, psi, sizeof(float2) * c->ncell * c->d.batch, where));
+  WDM_CU(c, cudaMemsetAsync(c->flag, 0, sizeof(int), c->st));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  c->have_psi = 1;
+  c->phi_valid = 0;
+  return WDM_OK;
+}
+
+wdm_status wdm_get_psi(wdm_ctx* c, void* psi, int32_t where) {
+  WDM_TRY(need_psi(c));
+  return copy_out(c, psi, c->psi, sizeof(float2) * c->ncell * c->d.batch, where);
+}
+
+wdm_status wdm_get_rho(wdm_ctx* c, float* rho, int32_t where) {
+  WDM_TRY(need_psi(c));
+  WDM_TRY(ensure_scratch(c));
+  cudaError_t e = launch_abs2(c->psi, c->scratch_f, c->ncell * c->d.batch, c->st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "abs2");
+  return copy_out(c, rho, c->scratch_f, sizeof(float) * c->ncell * c->d.batch, where);
+}
+
+static wdm_status phi_real(wdm_ctx* c) {
+  WDM_TRY(ensure_scratch(c));
+  if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, 0.0));
+  cudaError_t e = run_pass(c, P_PHI_OUT, [&] {
+    return c->kx->x_c2r(c->H, c->scratch_f, rows_psi(c), c->nxh, c->nhalf, c->twx, c->d.batch, c->st);
+  });
+  if (e != cudaSuccess) return cuda_fail(c, e, "x_c2r");
+  return WDM_OK;
+}
+
+wdm_status wdm_get_phi(wdm_ctx* c, float* phi, int32_t where) {
+  WDM_TRY(need_psi(c));
+  WDM_TRY(phi_real(c));
+  return copy_out(c, phi, c->scratch_f, sizeof(float) * c->ncell * c->d.batch, where);
+}
+
+wdm_status wdm_set_static_potential(wdm_ctx* c, const float* V, int32_t where) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (!V) {
+    if (c->V) cudaFree(c->V);
+    c->V = nullptr;
+    return WDM_OK;
+  }
+  if (!c->V) WDM_TRY(dalloc(c, &c->V, (size_t)c->ncell * c->d.batch));
+  WDM_TRY(copy_in(c, c->V, V, sizeof(float) * c->ncell * c->d.batch, where));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  return WDM_OK;
+}
+
+wdm_status wdm_set_tidal(wdm_ctx* c, const double* sched, int32_t nsched, int32_t per_item) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (nsched < 0) return fail(c, WDM_ERR_INVALID, "nsched < 0");
+  if (nsched == 0) {
+    c->tide_on = 0;
+    c->tide.clear();
+    return WDM_OK;
+  }
+  if (!sched) return fail(c, WDM_ERR_INVALID, "null tidal schedule");
+  if (per_item) {
+    if (nsched != c->d.batch) return fail(c, WDM_ERR_INVALID, "per-item tidal tensors need nsched == batch");
+    if (!c->T6b) WDM_TRY(dalloc(c, &c->T6b, (size_t)6 * c->d.batch));
+    std::vector<float> h((size_t)6 * nsched);
+    for (size_t i = 0; i < h.size(); ++i) h[i] = (float)sched[i];
+    WDM_CU(c, cudaMemcpyAsync(c->T6b, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    WDM_CU(c, cudaStreamSynchronize(c->st));
+    c->tide_on = 2;
+  } else {
+    c->tide.assign(sched, sched + (size_t)6 * nsched);
+    c->tide_on = 1;
+  }
+  return WDM_OK;
+}
+
+wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, int64_t n) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (n < 0) return fail(c, WDM_ERR_INVALID, "n < 0");
+  if (n > 0 && c->d.batch != 1) return fail(c, WDM_ERR_UNSUPPORTED, "baryon particles need batch == 1");
+  if (c->parts) cudaFree(c->parts);
+  c->parts = nullptr;
+  c->nparts = 0;
+  if (n == 0) return WDM_OK;
+  if (!pos || !mass) return fail(c, WDM_ERR_INVALID, "null particle arrays");
+  if (!c->rho_b) {
+    WDM_TRY(dalloc(c, &c->rho_b, (size_t)c->ncell));
+    WDM_CU(c, cudaMemsetAsync(c->rho_b, 0, sizeof(float) * c->ncell, c->st));
+  }
+  // cell index and fractions in FP64 on the host (particles are static)
+  std::vector<CicParticle> h((size_t)n);
+  const double d[3] = {c->dx, c->dy, c->dz};
+  const double o[3] = {c->x0, c->y0, c->z0};
+  const int nn[3] = {c->d.nx, c->d.ny, c->d.nz};
+  const double dV = c->dx * c->dy * c->dz;
+  for (int64_t p = 0; p < n; ++p) {
+    for (int a = 0; a < 3; ++a) {
+      const double u = (pos[3 * p + a] - o[a]) / d[a];
+      const double fl = std::floor(u);
+      long long i0 = (long long)fl % nn[a];
+      if (i0 < 0) i0 += nn[a];
+      h[p].i[a] = (int)i0;
+      h[p].f[a] = (float)(u - fl);
+    }
+    h[p].m = (float)(mass[p] / dV);
+  }
+  WDM_TRY(dalloc(c, &c->parts, (size_t)n));
+  WDM_CU(c, cudaMemcpyAsync(c->parts, h.data(), sizeof(CicParticle) * n, cudaMemcpyHostToDevice, c->st));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  c->nparts = n;
+  c->phi_valid = 0;
+  return WDM_OK;
+}
+
+static wdm_status step_impl(wdm_ctx* c, int32_t nsteps, double dt, double t0, int32_t mode) {
+  WDM_TRY(need_psi(c));
+  if (nsteps < 0) return fail(c, WDM_ERR_INVALID, "nsteps < 0");
+  if (!(std::isfinite(dt))) return fail(c, WDM_ERR_INVALID, "dt is not finite");
+  if (mode != WDM_STEP_STRANG && mode != WDM_STEP_REFERENCE_LOOP && mode != WDM_STEP_LIE)
+    return fail(c, WDM_ERR_INVALID, "unknown step mode");
+  if (c->tide_on == 1) {
+    const size_t need = (size_t)nsteps + 1;
+    const size_t have = c->tide.size() / 6;
+    if (have != 1 && have < need)
+      return fail(c, WDM_ERR_INVALID, "tidal schedule has " + std::to_string(have) + " rows, the step needs " +
+                                          std::to_string(need) + " (or exactly 1)");
+  }
+  (void)t0;
+  if (nsteps == 0) return WDM_OK;
+  if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
+  for (int s = 0; s < nsteps; ++s) {
+    double kdt;
+    if (mode == WDM_STEP_STRANG) kdt = (s == 0) ? 0.5 * dt : dt;  // interior half kicks merged
+    else if (mode == WDM_STEP_REFERENCE_LOOP) kdt = 0.5 * dt;
+    else kdt = dt;
+    WDM_TRY(kick(c, kdt, s, true));
+    WDM_TRY(drift_yz(c, dt));
+    WDM_TRY(density_poisson(c, 1, dt));
+  }
+  if (mode == WDM_STEP_STRANG) WDM_TRY(kick(c, 0.5 * dt, nsteps, false));
+  return WDM_OK;
+}
+
+wdm_status wdm_step_async(wdm_ctx* c, int32_t nsteps, double dt, double t0, int32_t mode) {
+  return step_impl(c, nsteps, dt, t0, mode);
+}
+
+wdm_status wdm_step(wdm_ctx* c, int32_t nsteps, double dt, double t0, int32_t mode) {
+  WDM_TRY(step_impl(c, nsteps, dt, t0, mode));
+  return sync_and_check(c);
+}
+
+wdm_status wdm_kick(wdm_ctx* c, double dt, double t) {
+  WDM_TRY(need_psi(c));
+  (void)t;
+  if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, 0.0));
+  WDM_TRY(kick(c, dt, 0, false));
+  return sync_and_check(c);
+}
+
+wdm_status wdm_drift(wdm_ctx* c, double dt) {
+  WDM_TRY(need_psi(c));
+  cudaError_t e = run_pass(c, P_X_FFT, [&] { return c->kx->xfft(c->psi, rows_psi(c), c->twx, false, 1.0f, c->d.batch, c->st); });
+  if (e != cudaSuccess) return cuda_fail(c, e, "x fwd");
+  WDM_TRY(drift_yz(c, dt));
+  WDM_TRY(density_poisson(c, 1, dt));
+  return sync_and_check(c);
+}
+
+wdm_status wdm_poisson(wdm_ctx* c, const float* rho, float* phi, int32_t where) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  WDM_TRY(ensure_scratch(c));
+  const int B = c->d.batch;
+  const size_t bytes = sizeof(float) * c->ncell * B;
+  const float* in = rho;
+  if (where == WDM_HOST) {
+    WDM_TRY(copy_in(c, c->scratch_f, rho, bytes, WDM_HOST));
+    in = c->scratch_f;
+  } else if (where != WDM_DEVICE) {
+    return fail(c, WDM_ERR_INVALID, "where must be WDM_HOST or WDM_DEVICE");
+  }
+  if (!in || !phi) return fail(c, WDM_ERR_INVALID, "null rho/phi");
+  cudaError_t e;
+  if ((e = c->kx->x_r2c(in, c->scratch_h, rows_psi(c), c->nxh, c->nhalf, c->twx, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "x r2c");
+  if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "y fwd");
+  PoissonOp po;
+  po.kx2 = c->kx2;
+  po.ky2 = c->ky2;
+  po.kz2 = c->kz2;
+  po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
+  po.nxa = c->nxh;
+  if ((e = c->kz->lfft_poisson(c->scratch_h, lines_z(c, c->nxh, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "z poisson");
+  if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "y inv");
+  float* dst = where == WDM_HOST ? c->scratch_f : phi;
+  if ((e = c->kx->x_c2r(c->scratch_h, dst, rows_psi(c), c->nxh, c->nhalf, c->twx, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "x c2r");
+  if (where == WDM_HOST) return copy_out(c, phi, c->scratch_f, bytes, WDM_HOST);
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  return WDM_OK;
+}
+
+wdm_status wdm_fft3d(wdm_ctx* c, void* data, int32_t dir) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (!data) return fail(c, WDM_ERR_INVALID, "null data");
+  if (dir != -1 && dir != 1) return fail(c, WDM_ERR_INVALID, "dir must be -1 or +1");
+  const bool inv = dir == 1;
+  const int B = c->d.batch;
+  float2* p = (float2*)data;
+  cudaError_t e;
+  if ((e = c->kx->xfft(p, rows_psi(c), c->twx, inv, 1.0f, B, c->st)) != cudaSuccess) return cuda_fail(c, e, "x");
+  if ((e = c->ky->lfft(p, lines_y(c, c->d.nx, c->ncell), c->twy, inv, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "y");
+  if ((e = c->kz->lfft(p, lines_z(c, c->d.nx, c->ncell), c->twz, inv, B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "z");
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  return WDM_OK;
+}
+
+wdm_status wdm_reduce(wdm_ctx* c, double* out) {
+  WDM_TRY(need_psi(c));
+  if (!out) return fail(c, WDM_ERR_INVALID, "null output");
+  WDM_TRY(phi_real(c));
+  RedGeom g;
+  g.nx = c->d.nx;
+  g.ny = c->d.ny;
+  g.nz = c->d.nz;
+  g.dx = c->dx;
+  g.dy = c->dy;
+  g.dz = c->dz;
+  g.x0 = c->x0;
+  g.y0 = c->y0;
+  g.z0 = c->z0;
+  cudaError_t e = launch_reduce(c->psi, c->scratch_f, g, c->red, c->red_blocks, c->d.batch, c->st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "reduce");
+  std::vector<double> h((size_t)c->red_blocks * RED_FIELDS * c->d.batch);
+  WDM_CU(c, cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  const double dV = c->dx * c->dy * c->dz;
+  for (int b = 0; b < c->d.batch; ++b) {
+    double acc[RED_FIELDS] = {0};
+    double best = -1.0, besti = 0;
+    for (int k = 0; k < c->red_blocks; ++k) {
+      const double* r = &h[((size_t)b * c->red_blocks + k) * RED_FIELDS];
+      for (int q = 0; q < RED_FIELDS; ++q)
+        if (q != RED_MAX && q != RED_ARG) acc[q] += r[q];
+      if (r[RED_MAX] > best || (r[RED_MAX] == best && r[RED_ARG] < besti)) {
+        best = r[RED_MAX];
+        besti = r[RED_ARG];
+      }
+    }
+    double* o = out + 10 * b;
+    const double m = acc[RED_MASS];
+    o[0] = m * dV;
+    o[1] = best;
+    o[2] = besti;
+    o[3] = m > 0 ? acc[RED_MX] / m : 0.0;
+    o[4] = m > 0 ? acc[RED_MY] / m : 0.0;
+    o[5] = m > 0 ? acc[RED_MZ] / m : 0.0;
+    const double W = -0.5 * acc[RED_W] * dV;
+    const double K = 0.5 * acc[RED_K] * dV;
+    const double Q = 0.5 * acc[RED_Q] * dV;
+    o[6] = W;
+    o[7] = K;
+    o[8] = Q;
+    o[9] = 2 * K + 2 * Q - W;
+  }
+  return WDM_OK;
+}
+
+wdm_status wdm_interpolate_phi(wdm_ctx* c, const double* pos, int64_t n, double* out) {
+  WDM_TRY(need_psi(c));
+  if (n < 0 || (n > 0 && (!pos || !out))) return fail(c, WDM_ERR_INVALID, "bad particle arrays");
+  if (n == 0) return WDM_OK;
+  if (c->d.batch != 1) return fail(c, WDM_ERR_UNSUPPORTED, "interpolation needs batch == 1");
+  WDM_TRY(phi_real(c));
+  std::vector<CicParticle> h((size_t)n);
+  const double d[3] = {c->dx, c->dy, c->dz};
+  const double o[3] = {c->x0, c->y0, c->z0};
+  const int nn[3] = {c->d.nx, c->d.ny, c->d.nz};
+  for (int64_t p = 0; p < n; ++p) {
+    for (int a = 0; a < 3; ++a) {
+      const double u = (pos[3 * p + a] - o[a]) / d[a];
+      const double fl = std::floor(u);
+      long long i0 = (long long)fl % nn[a];
+      if (i0 < 0) i0 += nn[a];
+      h[p].i[a] = (int)i0;
+      h[p].f[a] = (float)(u - fl);
+    }
+    h[p].m = 1.f;
+  }
+  CicParticle* dp = nullptr;
+  double* dout = nullptr;
+  WDM_TRY(dalloc(c, &dp, (size_t)n));
+  wdm_status s = dalloc(c, &dout, (size_t)n);
+  if (s != WDM_OK) {
+    cudaFree(dp);
+    return s;
+  }
+  cudaError_t e = cudaMemcpyAsync(dp, h.data(), sizeof(CicParticle) * n, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = launch_cic_interp(c->scratch_f, dp, n, c->d.nx, c->d.ny, c->d.nz, dout, c->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(dp);
+  cudaFree(dout);
+  if (e != cudaSuccess) return cuda_fail(c, e, "interpolate");
+  return WDM_OK;
+}
+
+int32_t wdm_num_passes(void) { return NPASS; }
+
+const char* wdm_pass_name(int32_t p) { return (p >= 0 && p < NPASS) ? PASS_NAMES[p] : ""; }
+
+int64_t wdm_launch_count(const wdm_ctx* c) { return c ? c->launch_count : 0; }
+
+wdm_status wdm_set_profiling(wdm_ctx* c, int32_t on) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  WDM_CU(c, prof_flush(c));
+  for (int p = 0; p < NPASS; ++p) {
+    c->prof.launches[p] = 0;
+    c->prof.ms[p] = 0.0;
+  }
+  c->prof.on = on != 0;
+  return WDM_OK;
+}
+
+wdm_status wdm_get_profile(wdm_ctx* c, int64_t* launches, double* ms, double* bytes) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  WDM_CU(c, prof_flush(c));
+  for (int p = 0; p < NPASS; ++p) {
+    if (launches) launches[p] = c->prof.launches[p];
+    if (ms) ms[p] = c->prof.ms[p];
+    if (bytes) bytes[p] = pass_bytes(c, p);
+  }
+  return WDM_OK;
+}
+
+wdm_status wdm_check_finite(wdm_ctx* c, int32_t* finite) {
+  WDM_TRY(need_psi(c));
+  if (!finite) return fail(c, WDM_ERR_INVALID, "null output");
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  int flag = 0;
+  WDM_CU(c, cudaMemcpy(&flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (fault_injected("nonfinite")) flag = 1;
+  *finite = flag ? 0 : 1;
+  return WDM_OK;
+}
+
+}  // extern "C"
