@@ -179,3 +179,52 @@ cudaError_t launch_cic_interp(const float* field, const CicParticle* p, long lon
 }
 
 }  // namespace wdm
+
+namespace wdm {
+
+// Mean of |psi|^2 (complex input) or of a float field, per batch item, as a
+// float shift: FP64 block partial sums, FP64 atomics into sums[b] (zeroed by
+// the launcher), then shift[b] = sums[b] / n + add.
+template <bool COMPLEX>
+__global__ void k_block_sum(const void* __restrict__ data, long long n, double* __restrict__ sums) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if constexpr (COMPLEX) {
+      const float2 v = static_cast<const float2*>(data)[blockIdx.y * n + i];
+      acc += (double)v.x * v.x + (double)v.y * v.y;
+    } else {
+      acc += (double)static_cast<const float*>(data)[blockIdx.y * n + i];
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
+    atomicAdd(sums + blockIdx.y, s);
+  }
+}
+
+__global__ void k_finalize_shift(const double* __restrict__ sums, float* __restrict__ shift, int batch, double inv_n,
+                                 double add) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) shift[b] = (float)(sums[b] * inv_n + add);
+}
+
+cudaError_t launch_mean_shift(const void* data, bool complex_in, long long n, int batch, double* sums, float* shift,
+                              double add, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(double) * batch, st);
+  if (e != cudaSuccess) return e;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 304) blocks = 304;
+  if (complex_in) k_block_sum<true><<<dim3((unsigned)blocks, batch), 256, 0, st>>>(data, n, sums);
+  else k_block_sum<false><<<dim3((unsigned)blocks, batch), 256, 0, st>>>(data, n, sums);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  k_finalize_shift<<<(batch + 127) / 128, 128, 0, st>>>(sums, shift, batch, 1.0 / (double)n, add);
+  return cudaGetLastError();
+}
+
+}  // namespace wdm

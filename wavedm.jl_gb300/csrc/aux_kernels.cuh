@@ -32,6 +32,9 @@ struct RedGeom {
 };
 
 cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t st);
+// shift[b] = mean over item b of |data|^2 (complex_in) or of data (float), + add
+cudaError_t launch_mean_shift(const void* data, bool complex_in, long long n, int batch, double* sums, float* shift,
+                              double add, cudaStream_t st);
 cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g, double* partials, int nblocks,
                           int batch, cudaStream_t st);
 cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz,

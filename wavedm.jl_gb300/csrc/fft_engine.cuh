@@ -18,8 +18,8 @@
 // plan's first stage reads: a forward transform, a pointwise k-space
 // multiply and the inverse transform therefore chain in registers.
 //
-// Twiddles come from a per-N table W_N^m (m < N) built in FP64 on the host and
-// rounded once to FP32.
+// Twiddles W_N^m are built in FP64 on the host and kept as FP32 (hi, lo)
+// pairs, in stage-major tables (see stage_compute).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -41,7 +41,22 @@ __device__ __forceinline__ float2 mul_i(float2 a) {
 
 // ----------------------------------------------------------------------------
 // small DFTs in registers (forward: exp(-2 pi i nk/R), inverse: exp(+...))
+//
+// The irrational butterfly constants sqrt(2)/2 and sqrt(3)/2 both round *down*
+// in FP32 (2 fl(sqrt2/2)^2 = 1 - 1.4e-8), which would shrink |psi| by a fixed
+// fraction at every butterfly and show up as a steady mass drift over
+// thousands of steps.  They are applied as a two-term product c_hi x + c_lo x
+// (c_lo = c - c_hi), leaving only the unbiased rounding of the result.
 // ----------------------------------------------------------------------------
+struct Const {
+  static constexpr float r_hi = 0.70710678118654752440f;  // sqrt(2)/2
+  static constexpr float r_lo = 1.2101617e-08f;           // sqrt(2)/2 - r_hi
+  static constexpr float h_hi = 0.86602540378443864676f;  // sqrt(3)/2
+  static constexpr float h_lo = 1.5543625e-08f;           // sqrt(3)/2 - h_hi
+};
+__device__ __forceinline__ float mul_r(float a) { return fmaf(a, Const::r_hi, a * Const::r_lo); }
+__device__ __forceinline__ float mul_h(float a) { return fmaf(a, Const::h_hi, a * Const::h_lo); }
+
 template <bool INV>
 __device__ __forceinline__ void dft2(float2* v) {
   float2 a = v[0], b = v[1];
@@ -51,11 +66,10 @@ __device__ __forceinline__ void dft2(float2* v) {
 
 template <bool INV>
 __device__ __forceinline__ void dft3(float2* v) {
-  const float h = 0.86602540378443864676f;  // sqrt(3)/2
   float2 a = v[0], b = v[1], c = v[2];
   float2 s = cadd(b, c), d = csub(b, c);
   float2 m = make_float2(fmaf(-0.5f, s.x, a.x), fmaf(-0.5f, s.y, a.y));
-  float2 r = mul_i<INV>(cscale(d, h));
+  float2 r = mul_i<INV>(make_float2(mul_h(d.x), mul_h(d.y)));
   v[0] = cadd(a, s);
   v[1] = cadd(m, r);
   v[2] = csub(m, r);
@@ -71,16 +85,14 @@ __device__ __forceinline__ void dft4(float2* v) {
   v[3] = csub(t1, t3);
 }
 
-// x * W8^1 (forward W8 = exp(-i pi/4))
+// x * W8^1 and x * W8^3 (forward W8 = exp(-i pi/4))
 template <bool INV>
 __device__ __forceinline__ float2 w8_1(float2 a) {
-  const float r = 0.70710678118654752440f;
-  return INV ? make_float2(r * (a.x - a.y), r * (a.x + a.y)) : make_float2(r * (a.x + a.y), r * (a.y - a.x));
+  return INV ? make_float2(mul_r(a.x - a.y), mul_r(a.x + a.y)) : make_float2(mul_r(a.x + a.y), mul_r(a.y - a.x));
 }
 template <bool INV>
 __device__ __forceinline__ float2 w8_3(float2 a) {
-  const float r = 0.70710678118654752440f;
-  return INV ? make_float2(-r * (a.x + a.y), r * (a.x - a.y)) : make_float2(r * (a.y - a.x), -r * (a.x + a.y));
+  return INV ? make_float2(-mul_r(a.x + a.y), mul_r(a.x - a.y)) : make_float2(mul_r(a.y - a.x), -mul_r(a.x + a.y));
 }
 
 template <bool INV>
@@ -107,11 +119,11 @@ __device__ __forceinline__ void dft6(float2* v) {
   float2 b[3] = {v[1], v[3], v[5]};
   dft3<INV>(a);
   dft3<INV>(b);
-  const float h = 0.86602540378443864676f;
-  // W6^1 = (1/2, -+h), W6^2 = (-1/2, -+h)
+  // W6^1 = (1/2, -+h), W6^2 = (-1/2, -+h); sg = -1 forward, +1 inverse
   const float sg = INV ? 1.f : -1.f;
-  b[1] = cmul(b[1], make_float2(0.5f, sg * h));
-  b[2] = cmul(b[2], make_float2(-0.5f, sg * h));
+  const float2 b1 = b[1], b2 = b[2];
+  b[1] = make_float2(fmaf(0.5f, b1.x, -sg * mul_h(b1.y)), fmaf(0.5f, b1.y, sg * mul_h(b1.x)));
+  b[2] = make_float2(fmaf(-0.5f, b2.x, -sg * mul_h(b2.y)), fmaf(-0.5f, b2.y, sg * mul_h(b2.x)));
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     v[k] = cadd(a[k], b[k]);
@@ -194,8 +206,28 @@ struct RadInfo<Radices<Rs...>> {
 // ----------------------------------------------------------------------------
 // stages
 // ----------------------------------------------------------------------------
-template <int N, int T, int R, int NS, bool INV>
-__device__ __forceinline__ void stage_compute(float2* v, const float2* __restrict__ tw, int t) {
+// Twiddle W = (x, y) + (z, w): FP32 nearest value plus its FP32 remainder
+// from the FP64 value, so the rotation is exact up to one rounding of the
+// result.  A plain FP32 table rounds each |W| slightly off 1 in a fixed way
+// and the mean of those errors compounds into a mass drift step after step.
+// The small correction terms are formed first and the large products are
+// added last: a correction added to an already rounded FP32 product is
+// smaller than half its ulp and would round straight back, leaving the
+// twiddle's modulus error (and the drift it causes) in place.
+__device__ __forceinline__ float2 twiddle_mul(float2 a, float4 w, bool inv) {
+  const float wy = inv ? -w.y : w.y, ly = inv ? -w.w : w.w;
+  const float cx = fmaf(a.x, w.z, -a.y * ly);
+  const float cy = fmaf(a.x, ly, a.y * w.z);
+  return make_float2(fmaf(a.x, w.x, fmaf(-a.y, wy, cx)), fmaf(a.x, wy, fmaf(a.y, w.x, cy)));
+}
+
+// Stage twiddles are laid out per stage as [jm][k-1] (jm < NS, 1 <= k < R),
+// stage after stage in the plan's radix order: stage s starts at OFF = sum of
+// NS (R - 1) over the earlier stages (N - 1 entries in all).  Lanes that run
+// consecutive butterflies then read consecutive entries, which keeps the
+// per-lane twiddle loads of the warp-per-line passes free of bank conflicts.
+template <int N, int T, int R, int NS, bool INV, int OFF>
+__device__ __forceinline__ void stage_compute(float2* v, const float4* __restrict__ tw, int t) {
   constexpr int NB = N / (R * T);
   static_assert(NB * R * T == N, "plan: T must divide N/R");
 #pragma unroll
@@ -203,21 +235,35 @@ __device__ __forceinline__ void stage_compute(float2* v, const float2* __restric
     if constexpr (NS > 1) {
       const int j = t + T * i;
       const int jm = j % NS;
-      constexpr int STEP = N / (NS * R);
+      const float4* w = tw + OFF + jm * (R - 1);
 #pragma unroll
-      for (int k = 1; k < R; ++k) {
-        float2 w = tw[k * jm * STEP];
-        if (INV) w.y = -w.y;
-        v[i * R + k] = cmul(v[i * R + k], w);
-      }
+      for (int k = 1; k < R; ++k) v[i * R + k] = twiddle_mul(v[i * R + k], w[k - 1], INV);
     }
     dftR<R, INV>(v + i * R);
   }
 }
 
-template <int N, int T, int R, int NS, int LP>
+// Host-side builder of the stage-major twiddle table of a radix order
+// (W_N^m in FP64, stored as FP32 hi + lo); writes N - 1 entries.
+template <int N, class TW, class F, int... Rs>
+inline void fill_stage_twiddles(Radices<Rs...>, TW* out, F make) {
+  const int radices[] = {Rs...};
+  int ns = 1, off = 0;
+  for (int R : radices) {
+    for (int jm = 0; jm < ns; ++jm)
+      for (int k = 1; k < R; ++k) out[off + jm * (R - 1) + (k - 1)] = make((long long)k * jm * (N / (ns * R)));
+    off += ns * (R - 1);
+    ns *= R;
+  }
+}
+
+// Exchange writes/reads.  Line slots l >= LACT are idle (their registers hold
+// don't-care values) and touch no shared memory, so a buffer with pitch LP can
+// serve LACT < LP lines.
+template <int N, int T, int R, int NS, int LP, int LACT = (1 << 30)>
 __device__ __forceinline__ void stage_write(float2* s, const float2* v, int t, int l) {
   constexpr int NB = N / (R * T);
+  if (l >= LACT) return;
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     const int j = t + T * i;
@@ -227,9 +273,10 @@ __device__ __forceinline__ void stage_write(float2* s, const float2* v, int t, i
   }
 }
 
-template <int N, int T, int R, int LP>
+template <int N, int T, int R, int LP, int LACT = (1 << 30)>
 __device__ __forceinline__ void stage_read(const float2* s, float2* v, int t, int l) {
   constexpr int NB = N / (R * T);
+  if (l >= LACT) return;
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     const int j = t + T * i;
@@ -238,23 +285,38 @@ __device__ __forceinline__ void stage_read(const float2* s, float2* v, int t, in
   }
 }
 
-template <int N, int T, int LP, bool INV, int NS, int R, int... Rest>
-__device__ __forceinline__ void run_stages_impl(float2* v, float2* s, const float2* tw, int t, int l) {
-  stage_compute<N, T, R, NS, INV>(v, tw, t);
+template <int N, int T, int LP, bool INV, int LACT, int NS, int OFF, int R, int... Rest>
+__device__ __forceinline__ void run_stages_impl(float2* v, float2* s, const float4* tw, int t, int l) {
+  stage_compute<N, T, R, NS, INV, OFF>(v, tw, t);
   if constexpr (sizeof...(Rest) > 0) {
     constexpr int RN = First<Rest...>::value;
     __syncthreads();
-    stage_write<N, T, R, NS, LP>(s, v, t, l);
+    stage_write<N, T, R, NS, LP, LACT>(s, v, t, l);
     __syncthreads();
-    stage_read<N, T, RN, LP>(s, v, t, l);
-    run_stages_impl<N, T, LP, INV, NS * R, Rest...>(v, s, tw, t, l);
+    stage_read<N, T, RN, LP, LACT>(s, v, t, l);
+    run_stages_impl<N, T, LP, INV, LACT, NS * R, OFF + NS * (R - 1), Rest...>(v, s, tw, t, l);
   }
 }
 
+// tw: the stage-major table of this radix order
 template <int N, int T, int LP, bool INV, int... Rs>
-__device__ __forceinline__ void run_stages(Radices<Rs...>, float2* v, float2* s, const float2* tw, int t, int l) {
-  run_stages_impl<N, T, LP, INV, 1, Rs...>(v, s, tw, t, l);
+__device__ __forceinline__ void run_stages(Radices<Rs...>, float2* v, float2* s, const float4* tw, int t, int l) {
+  run_stages_impl<N, T, LP, INV, (1 << 30), 1, 0, Rs...>(v, s, tw, t, l);
 }
+
+// Same with only line slots l < LACT exchanging through s.
+template <int N, int T, int LP, bool INV, int LACT, int... Rs>
+__device__ __forceinline__ void run_stages_act(Radices<Rs...>, float2* v, float2* s, const float4* tw, int t, int l) {
+  run_stages_impl<N, T, LP, INV, LACT, 1, 0, Rs...>(v, s, tw, t, l);
+}
+
+// cp.async: 8-byte global -> shared copies that do not pass through registers
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Position along the line of register slot (i, k) before the first stage of
 // radix R (the load pattern) or after the last stage of radix R (the store
@@ -262,10 +324,13 @@ __device__ __forceinline__ void run_stages(Radices<Rs...>, float2* v, float2* s,
 template <int N, int T, int R>
 __device__ __forceinline__ int slot_pos(int t, int i, int k) { return t + T * i + k * (N / R); }
 
-// Load the twiddle table of length N into shared memory.
-template <int N>
-__device__ __forceinline__ void load_twiddles(float2* tw_s, const float2* __restrict__ tw_g) {
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw_s[i] = tw_g[i];
+// Load `count` entries of a (hi, lo) twiddle table into shared memory.
+__device__ __forceinline__ void load_twiddles(float4* tw_s, const float4* __restrict__ tw_g, int count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) tw_s[i] = tw_g[i];
 }
+
+// Per-axis twiddle tables (N entries each, N - 1 used): the line passes'
+// radix order and its reverse, then the x passes' order and its reverse.
+enum { TW_LINE_FWD = 0, TW_LINE_REV = 1, TW_X_FWD = 2, TW_X_REV = 3, TW_TABLES = 4 };
 
 }  // namespace wdm

@@ -1,6 +1,8 @@
 // Launchers of the pass kernels for one axis length N (included by sizes_*.cu).
 #pragma once
+#include <cmath>
 #include "kernel_set.h"
+#include "xpass_warp.cuh"
 
 namespace wdm {
 
@@ -16,10 +18,11 @@ template <int N>
 struct Launch {
   static constexpr int NT = threads_for<N>();
   static constexpr size_t SM = smem_bytes<N>();
+  static constexpr size_t SMID = smem_bytes_mid<N>();
 
   static dim3 grid_lines(int nlines, int batch) { return dim3((nlines + LINES - 1) / LINES, batch); }
 
-  static cudaError_t lfft(float2* data, const LineGeom& g, const float2* tw, bool inv, int batch, cudaStream_t st) {
+  static cudaError_t lfft(float2* data, const LineGeom& g, const float4* tw, bool inv, int batch, cudaStream_t st) {
     if (g.nlines <= 0) return cudaSuccess;
     cudaError_t e;
     if (inv) {
@@ -31,67 +34,106 @@ struct Launch {
     }
     return cudaGetLastError();
   }
-  static cudaError_t lfft_drift(float2* data, const LineGeom& g, const float2* tw, const DriftOp& op, int batch,
+  static cudaError_t lfft_drift(float2* data, const LineGeom& g, const float4* tw, const DriftOp& op, int batch,
                                 cudaStream_t st) {
     cudaError_t e;
-    if ((e = prep_once<k_lfft_mid<N, DriftOp>>(SM)) != cudaSuccess) return e;
-    k_lfft_mid<N, DriftOp><<<grid_lines(g.nlines, batch), NT, SM, st>>>(data, g, tw, op);
+    if ((e = prep_once<k_lfft_mid<N, DriftOp>>(SMID)) != cudaSuccess) return e;
+    k_lfft_mid<N, DriftOp><<<grid_lines(g.nlines, batch), NT, SMID, st>>>(data, g, tw, op);
     return cudaGetLastError();
   }
-  static cudaError_t lfft_poisson(float2* data, const LineGeom& g, const float2* tw, const PoissonOp& op, int batch,
+  static cudaError_t lfft_poisson(float2* data, const LineGeom& g, const float4* tw, const PoissonOp& op, int batch,
                                   cudaStream_t st) {
     cudaError_t e;
-    if ((e = prep_once<k_lfft_mid<N, PoissonOp>>(SM)) != cudaSuccess) return e;
-    k_lfft_mid<N, PoissonOp><<<grid_lines(g.nlines, batch), NT, SM, st>>>(data, g, tw, op);
+    if ((e = prep_once<k_lfft_mid<N, PoissonOp>>(SMID)) != cudaSuccess) return e;
+    k_lfft_mid<N, PoissonOp><<<grid_lines(g.nlines, batch), NT, SMID, st>>>(data, g, tw, op);
     return cudaGetLastError();
   }
-  static cudaError_t xfft(float2* data, const RowGeom& rg, const float2* tw, bool inv, float scale, int batch,
+  // x passes: lane group per row pair, grid-stride over warp units
+  static constexpr int XNT = XCfg<N>::NT;
+  static constexpr size_t XSMEM = XCfg<N>::SMEM;
+  static dim3 grid_x(const RowGeom& rg, int batch, XWork* w) {
+    w->pairs_per_item = rg.nrows / 2;
+    w->batch = batch;
+    const long long pairs = (long long)w->pairs_per_item * batch;
+    const long long units = (pairs + XCfg<N>::GROUPS - 1) / XCfg<N>::GROUPS;
+    long long ctas = (units + XCfg<N>::WARPS - 1) / XCfg<N>::WARPS;
+    const long long cap = 152LL * 6;
+    return dim3((unsigned)(ctas < cap ? ctas : cap));
+  }
+  static cudaError_t xfft(float2* data, const RowGeom& rg, const float4* tw, bool inv, float scale, int batch,
                           cudaStream_t st) {
     cudaError_t e;
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
     if (inv) {
-      if ((e = prep_once<k_xfft<N, true>>(SM)) != cudaSuccess) return e;
-      k_xfft<N, true><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(data, rg, tw, scale);
+      if ((e = prep_once<k_xw_fft<N, true>>(XSMEM)) != cudaSuccess) return e;
+      k_xw_fft<N, true><<<gr, XNT, XSMEM, st>>>(data, rg, tw, scale, w);
     } else {
-      if ((e = prep_once<k_xfft<N, false>>(SM)) != cudaSuccess) return e;
-      k_xfft<N, false><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(data, rg, tw, scale);
+      if ((e = prep_once<k_xw_fft<N, false>>(XSMEM)) != cudaSuccess) return e;
+      k_xw_fft<N, false><<<gr, XNT, XSMEM, st>>>(data, rg, tw, scale, w);
     }
     return cudaGetLastError();
   }
   static cudaError_t x_inv_rho(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                               const float2* tw, const RhoArgs& a, int batch, cudaStream_t st) {
+                               const float4* tw, const RhoArgs& a, int batch, cudaStream_t st) {
     cudaError_t e;
-    if ((e = prep_once<k_x_inv_rho<N>>(SM)) != cudaSuccess) return e;
-    k_x_inv_rho<N><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(psi, H, rg, hpitch, hbstride, tw, a);
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
+    if ((e = prep_once<k_xw_inv_rho<N>>(XSMEM)) != cudaSuccess) return e;
+    k_xw_inv_rho<N><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
     return cudaGetLastError();
   }
   static cudaError_t x_kick(float2* psi, const float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                            const float2* tw, const KickArgs& a, bool fwd, int batch, cudaStream_t st) {
+                            const float4* tw, const KickArgs& a, bool fwd, int batch, cudaStream_t st) {
     cudaError_t e;
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
     if (fwd) {
-      if ((e = prep_once<k_x_kick<N, true>>(SM)) != cudaSuccess) return e;
-      k_x_kick<N, true><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(psi, H, rg, hpitch, hbstride, tw, a);
+      if ((e = prep_once<k_xw_kick<N, true>>(XSMEM)) != cudaSuccess) return e;
+      k_xw_kick<N, true><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
     } else {
-      if ((e = prep_once<k_x_kick<N, false>>(SM)) != cudaSuccess) return e;
-      k_x_kick<N, false><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(psi, H, rg, hpitch, hbstride, tw, a);
+      if ((e = prep_once<k_xw_kick<N, false>>(XSMEM)) != cudaSuccess) return e;
+      k_xw_kick<N, false><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
     }
     return cudaGetLastError();
   }
   static cudaError_t x_c2r(const float2* H, float* out, const RowGeom& rg, long long hpitch, long long hbstride,
-                           const float2* tw, int batch, cudaStream_t st) {
+                           const float4* tw, int batch, cudaStream_t st) {
     cudaError_t e;
-    if ((e = prep_once<k_x_c2r<N>>(SM)) != cudaSuccess) return e;
-    k_x_c2r<N><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(H, out, rg, hpitch, hbstride, tw);
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
+    if ((e = prep_once<k_xw_c2r<N>>(XSMEM)) != cudaSuccess) return e;
+    k_xw_c2r<N><<<gr, XNT, XSMEM, st>>>(H, out, rg, hpitch, hbstride, tw, w);
     return cudaGetLastError();
   }
   static cudaError_t x_r2c(const float* in, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                           const float2* tw, int batch, cudaStream_t st) {
+                           const float4* tw, const float* shift, int batch, cudaStream_t st) {
     cudaError_t e;
-    if ((e = prep_once<k_x_r2c<N>>(SM)) != cudaSuccess) return e;
-    k_x_r2c<N><<<grid_lines(rg.nrows, batch), NT, SM, st>>>(in, H, rg, hpitch, hbstride, tw);
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
+    if ((e = prep_once<k_xw_r2c<N>>(XSMEM)) != cudaSuccess) return e;
+    k_xw_r2c<N><<<gr, XNT, XSMEM, st>>>(in, H, rg, hpitch, hbstride, tw, shift, w);
     return cudaGetLastError();
   }
+  // host: the four stage-major twiddle tables of this axis length (TW_TABLES x N)
+  static void fill_twiddles(float4* out) {
+    auto make = [](long long m) {
+      const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)N;
+      const double cr = std::cos(a), ci = std::sin(a);
+      const float hr = (float)cr, hi = (float)ci;
+      return make_float4(hr, hi, (float)(cr - (double)hr), (float)(ci - (double)hi));
+    };
+    for (int q = 0; q < TW_TABLES * N; ++q) out[q] = make_float4(1.f, 0.f, 0.f, 0.f);
+    using LF = typename Plan<N>::Fwd;
+    using XF = typename XPlan<N>::Fwd;
+    fill_stage_twiddles<N>(LF{}, out + TW_LINE_FWD * N, make);
+    fill_stage_twiddles<N>(typename Reverse<LF>::type{}, out + TW_LINE_REV * N, make);
+    fill_stage_twiddles<N>(XF{}, out + TW_X_FWD * N, make);
+    fill_stage_twiddles<N>(typename Reverse<XF>::type{}, out + TW_X_REV * N, make);
+  }
   static const KernelSet* set() {
-    static const KernelSet ks = {N, &lfft, &lfft_drift, &lfft_poisson, &xfft, &x_inv_rho, &x_kick, &x_c2r, &x_r2c};
+    static const KernelSet ks = {N, &lfft, &lfft_drift, &lfft_poisson, &xfft, &x_inv_rho, &x_kick, &x_c2r, &x_r2c,
+                                 &fill_twiddles};
     return &ks;
   }
 };

@@ -10,22 +10,24 @@ namespace wdm {
 struct KernelSet {
   int n;
   // strided lines (y or z axis), C2C in place
-  cudaError_t (*lfft)(float2* data, const LineGeom& g, const float2* tw, bool inv, int batch, cudaStream_t st);
-  cudaError_t (*lfft_drift)(float2* data, const LineGeom& g, const float2* tw, const DriftOp& op, int batch,
+  cudaError_t (*lfft)(float2* data, const LineGeom& g, const float4* tw, bool inv, int batch, cudaStream_t st);
+  cudaError_t (*lfft_drift)(float2* data, const LineGeom& g, const float4* tw, const DriftOp& op, int batch,
                             cudaStream_t st);
-  cudaError_t (*lfft_poisson)(float2* data, const LineGeom& g, const float2* tw, const PoissonOp& op, int batch,
+  cudaError_t (*lfft_poisson)(float2* data, const LineGeom& g, const float4* tw, const PoissonOp& op, int batch,
                               cudaStream_t st);
   // contiguous rows (x axis)
-  cudaError_t (*xfft)(float2* data, const RowGeom& rg, const float2* tw, bool inv, float scale, int batch,
+  cudaError_t (*xfft)(float2* data, const RowGeom& rg, const float4* tw, bool inv, float scale, int batch,
                       cudaStream_t st);
   cudaError_t (*x_inv_rho)(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                           const float2* tw, const RhoArgs& a, int batch, cudaStream_t st);
+                           const float4* tw, const RhoArgs& a, int batch, cudaStream_t st);
   cudaError_t (*x_kick)(float2* psi, const float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                        const float2* tw, const KickArgs& a, bool fwd, int batch, cudaStream_t st);
+                        const float4* tw, const KickArgs& a, bool fwd, int batch, cudaStream_t st);
   cudaError_t (*x_c2r)(const float2* H, float* out, const RowGeom& rg, long long hpitch, long long hbstride,
-                       const float2* tw, int batch, cudaStream_t st);
+                       const float4* tw, int batch, cudaStream_t st);
   cudaError_t (*x_r2c)(const float* in, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                       const float2* tw, int batch, cudaStream_t st);
+                       const float4* tw, const float* shift, int batch, cudaStream_t st);
+  // host: fill the TW_TABLES x n stage-major twiddle tables of this axis length
+  void (*fill_twiddles)(float4* out);
 };
 
 const KernelSet* kernels_for(int n);

@@ -96,7 +96,7 @@ struct wdm_ctx {
   // device buffers
   float2* psi = nullptr;
   float2* H = nullptr;
-  float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  float4 *twx = nullptr, *twy = nullptr, *twz = nullptr;  // (hi, lo) twiddles
   float *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
   float2 *cx = nullptr, *cy = nullptr, *cz = nullptr;  // precise drift tables (cached per dt)
   double tab_dt = NAN;
@@ -114,6 +114,10 @@ struct wdm_ctx {
   float2* scratch_h = nullptr;      // half-spectrum scratch
   double* red = nullptr;            // reduction partials
   int red_blocks = 0;
+  double* sums = nullptr;           // [batch] FP64 sums for the density shift
+  float* shift = nullptr;           // [batch] estimate of <rho> subtracted before the R2C (psi path)
+  float* shift_in = nullptr;        // [batch] mean of a wdm_poisson input
+  double rho_b_mean = 0.0;          // mean baryon density (static particles)
   int have_psi = 0;
   int phi_valid = 0;
   int64_t launch_count = 0;
@@ -245,14 +249,13 @@ static double kval(int m, int n, double L) {
   return 2.0 * M_PI * s / L;
 }
 
-static wdm_status upload_twiddles(wdm_ctx* c, float2** dst, int n) {
-  std::vector<float2> h(n);
-  for (int m = 0; m < n; ++m) {
-    const double a = -2.0 * M_PI * (double)m / (double)n;
-    h[m] = make_float2((float)std::cos(a), (float)std::sin(a));
-  }
-  WDM_TRY(dalloc(c, dst, n));
-  WDM_CU(c, cudaMemcpy(*dst, h.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
+// The four stage-major (hi, lo) twiddle tables of an axis (TW_TABLES x n).
+static wdm_status upload_twiddles(wdm_ctx* c, float4** dst, const KernelSet* ks) {
+  const int n = ks->n;
+  std::vector<float4> h((size_t)TW_TABLES * n);
+  ks->fill_twiddles(h.data());
+  WDM_TRY(dalloc(c, dst, h.size()));
+  WDM_CU(c, cudaMemcpy(*dst, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice));
   return WDM_OK;
 }
 
@@ -267,21 +270,22 @@ static wdm_status upload_k2(wdm_ctx* c, float** dst, int n, double L) {
   return WDM_OK;
 }
 
-// Drift phase tables exp(-i k_a^2 dt/2) built in FP64 (argument reduced mod 2pi
-// in double before cos/sin); the z table carries 1/(nx ny nz).
+// Drift phase tables exp(-i k_a^2 dt/2) - 1 built in FP64 (argument reduced mod
+// 2 pi in double before sin).
 static wdm_status ensure_drift_tables(wdm_ctx* c, double dt) {
   if (c->tab_dt == dt) return WDM_OK;
   const int n[3] = {c->d.nx, c->d.ny, c->d.nz};
   const double L[3] = {c->d.lx, c->d.ly, c->d.lz};
   float2* dst[3] = {c->cx, c->cy, c->cz};
-  const double scale = 1.0 / ((double)c->d.nx * c->d.ny * c->d.nz);
   for (int a = 0; a < 3; ++a) {
     std::vector<float2> h(n[a]);
     for (int m = 0; m < n[a]; ++m) {
+      // th = k^2 dt/2 reduced to [0, 2 pi) in FP64, kept as FP32 hi + lo
       const double k = kval(m, n[a], L[a]);
-      const double th = std::fmod(0.5 * k * k * dt, 2.0 * M_PI);
-      const double s = (a == 2) ? scale : 1.0;
-      h[m] = make_float2((float)(s * std::cos(th)), (float)(-s * std::sin(th)));
+      double th = std::fmod(0.5 * k * k * dt, 2.0 * M_PI);
+      if (th < 0) th += 2.0 * M_PI;
+      const float hi = (float)th;
+      h[m] = make_float2(hi, (float)(th - (double)hi));
     }
     WDM_CU(c, cudaMemcpyAsync(dst[a], h.data(), n[a] * sizeof(float2), cudaMemcpyHostToDevice, c->st));
     WDM_CU(c, cudaStreamSynchronize(c->st));
@@ -367,6 +371,7 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.rb_bstride = 0;
   ra.write_psi = write_psi;
   ra.nonfinite = c->flag;
+  ra.shift = c->shift;
   cudaError_t e = run_pass(c, write_psi ? P_X_INV_RHO : P_DENSITY, [&] {
     return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, ra, B, c->st);
   });
@@ -451,7 +456,9 @@ static wdm_status drift_yz(wdm_ctx* c, double dt) {
   op.ky2 = c->ky2;
   op.kz2 = c->kz2;
   op.half_dt = (float)(0.5 * dt);
-  op.scale = (float)(1.0 / ((double)c->d.nx * c->d.ny * c->d.nz));
+  const double scale = 1.0 / ((double)c->d.nx * c->d.ny * c->d.nz);
+  op.scale = (float)scale;
+  op.scale_lo = (float)(scale - (double)op.scale);
   op.nxa = c->d.nx;
   op.precise = precise;
   op.tab_bstride = 0;
@@ -509,6 +516,14 @@ static wdm_status ensure_scratch(wdm_ctx* c) {
   return WDM_OK;
 }
 
+// shift[b] = <|psi_b|^2> + mean baryon density: the constant removed from rho
+// before its transform (exact for any value: only k = 0 changes).
+static wdm_status update_shift(wdm_ctx* c) {
+  cudaError_t e = launch_mean_shift(c->psi, true, c->ncell, c->d.batch, c->sums, c->shift, c->rho_b_mean, c->st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "mean shift");
+  return WDM_OK;
+}
+
 // --------------------------------------------------------------------------
 // C ABI
 // --------------------------------------------------------------------------
@@ -527,7 +542,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
                   c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->parts, c->T6b, c->flag, c->scratch_f,
-                  c->scratch_h, c->red};
+                  c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (auto& r : c->prof.pending) {
@@ -582,9 +597,9 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   const size_t B = (size_t)d->batch;
   if ((s = dalloc(c, &c->psi, B * ncell)) != WDM_OK) return bail(s);
   if ((s = dalloc(c, &c->H, B * c->nhalf)) != WDM_OK) return bail(s);
-  if ((s = upload_twiddles(c, &c->twx, d->nx)) != WDM_OK) return bail(s);
-  if ((s = upload_twiddles(c, &c->twy, d->ny)) != WDM_OK) return bail(s);
-  if ((s = upload_twiddles(c, &c->twz, d->nz)) != WDM_OK) return bail(s);
+  if ((s = upload_twiddles(c, &c->twx, c->kx)) != WDM_OK) return bail(s);
+  if ((s = upload_twiddles(c, &c->twy, c->ky)) != WDM_OK) return bail(s);
+  if ((s = upload_twiddles(c, &c->twz, c->kz)) != WDM_OK) return bail(s);
   if ((s = upload_k2(c, &c->kx2, d->nx, d->lx)) != WDM_OK) return bail(s);
   if ((s = upload_k2(c, &c->ky2, d->ny, d->ly)) != WDM_OK) return bail(s);
   if ((s = upload_k2(c, &c->kz2, d->nz, d->lz)) != WDM_OK) return bail(s);
@@ -601,6 +616,13 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   }
   c->red_blocks = 4 * 152;
   if ((s = dalloc(c, &c->red, B * c->red_blocks * RED_FIELDS)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->sums, B)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->shift, B)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->shift_in, B)) != WDM_OK) return bail(s);
+  if ((e = cudaMemsetAsync(c->shift, 0, sizeof(float) * B, c->st)) != cudaSuccess) {
+    cuda_fail(c, e, "memset shift");
+    return bail(WDM_ERR_CUDA);
+  }
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) {
     cuda_fail(c, e, "sync");
     return bail(WDM_ERR_CUDA);
@@ -614,6 +636,7 @@ wdm_status wdm_set_psi(wdm_ctx* c, const void* psi, int32_t where) {
   WDM_TRY(copy_in(c, c->psi, psi, sizeof(float2) * c->ncell * c->d.batch, where));
   WDM_CU(c, cudaMemsetAsync(c->flag, 0, sizeof(int), c->st));
   WDM_CU(c, cudaStreamSynchronize(c->st));
+  WDM_TRY(update_shift(c));
   c->have_psi = 1;
   c->phi_valid = 0;
   return WDM_OK;
@@ -719,6 +742,10 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
   WDM_CU(c, cudaMemcpyAsync(c->parts, h.data(), sizeof(CicParticle) * n, cudaMemcpyHostToDevice, c->st));
   WDM_CU(c, cudaStreamSynchronize(c->st));
   c->nparts = n;
+  double msum = 0.0;
+  for (int64_t p = 0; p < n; ++p) msum += mass[p];
+  c->rho_b_mean = msum / ((double)c->ncell * dV);
+  if (c->have_psi) WDM_TRY(update_shift(c));
   c->phi_valid = 0;
   return WDM_OK;
 }
@@ -792,7 +819,9 @@ wdm_status wdm_poisson(wdm_ctx* c, const float* rho, float* phi, int32_t where) 
   }
   if (!in || !phi) return fail(c, WDM_ERR_INVALID, "null rho/phi");
   cudaError_t e;
-  if ((e = c->kx->x_r2c(in, c->scratch_h, rows_psi(c), c->nxh, c->nhalf, c->twx, B, c->st)) != cudaSuccess)
+  if ((e = launch_mean_shift(in, false, c->ncell, B, c->sums, c->shift_in, 0.0, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "mean");
+  if ((e = c->kx->x_r2c(in, c->scratch_h, rows_psi(c), c->nxh, c->nhalf, c->twx, c->shift_in, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "x r2c");
   if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "y fwd");

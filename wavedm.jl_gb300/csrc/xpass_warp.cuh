@@ -1,0 +1,472 @@
+// x-axis (contiguous rows) passes, one lane group per row pair.
+//
+// A lane group is T = Plan<N>::T consecutive lanes of a warp (T divides 32).
+// It owns a pair of rows (A, B) = (2p, 2p+1): it transforms row A, then row
+// B, each straight from and back to global memory (lane t touches points
+// t + T m, so every access is a coalesced run along x), and transforms the
+// two real rows of the density / potential together as the complex line
+// A + iB.  Exchanges between radix stages go through the group's own padded
+// shared buffer with __syncwarp only: no CTA-wide barrier after the twiddle
+// table is loaded, so warps run independently and hide each other's latency.
+#pragma once
+#include "passes.cuh"
+
+namespace wdm {
+
+// Exchange buffer addressing: point p of a group lives at word base + p +
+// (p >> SH).  The shift SH of each stage boundary is chosen at compile time
+// by simulating the shared-memory banks of that boundary's write pattern (the
+// Stockham scatter of radix R at stride NS) and the next stage's read pattern
+// for the 32 lanes of a warp (8-byte words, 16 lanes per wavefront).
+__host__ __device__ constexpr int xbank_degree16(const int* a) {
+  int worst = 1;
+  for (int x = 0; x < 16; ++x) {
+    int d = 0;
+    for (int y = 0; y < 16; ++y) {
+      if (((a[y] - a[x]) & 15) != 0) continue;
+      bool dup = false;
+      for (int z = 0; z < y; ++z)
+        if (a[z] == a[y]) dup = true;
+      if (!dup) ++d;
+    }
+    if (d > worst) worst = d;
+  }
+  return worst;
+}
+
+template <int N, int T, int NP>
+struct XPad {
+  __host__ __device__ static constexpr int cost(int R, int NS, int RN, int sh) {
+    int total = 0;
+    for (int i = 0; i < N / (R * T); ++i)
+      for (int k = 0; k < R; ++k)
+        for (int half = 0; half < 2; ++half) {
+          int a[16] = {};
+          for (int q = 0; q < 16; ++q) {
+            const int lane = half * 16 + q, g = lane / T, t = lane % T, j = t + T * i;
+            const int p = (j / NS) * NS * R + (j % NS) + k * NS;
+            a[q] = g * NP + p + (p >> sh);
+          }
+          total += xbank_degree16(a);
+        }
+    for (int i = 0; i < N / (RN * T); ++i)
+      for (int k = 0; k < RN; ++k)
+        for (int half = 0; half < 2; ++half) {
+          int a[16] = {};
+          for (int q = 0; q < 16; ++q) {
+            const int lane = half * 16 + q, g = lane / T, t = lane % T, j = t + T * i;
+            const int p = j + k * (N / RN);
+            a[q] = g * NP + p + (p >> sh);
+          }
+          total += xbank_degree16(a);
+        }
+    return total;
+  }
+  __host__ __device__ static constexpr int best(int R, int NS, int RN) {
+    int bs = 30, bc = cost(R, NS, RN, 30);  // shift 30: no padding
+    for (int sh = 2; sh <= 6; ++sh) {
+      const int c = cost(R, NS, RN, sh);
+      if (c < bc) {
+        bc = c;
+        bs = sh;
+      }
+    }
+    return bs;
+  }
+};
+
+template <int N, int T, int R, int NS, int SH>
+__device__ __forceinline__ void wstage_write(float2* b, const float2* v, int t) {
+  constexpr int NB = N / (R * T);
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    const int j = t + T * i;
+    const int base = (j / NS) * NS * R + (j % NS);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int p = base + k * NS;
+      b[p + (p >> SH)] = v[i * R + k];
+    }
+  }
+}
+
+template <int N, int T, int R, int SH>
+__device__ __forceinline__ void wstage_read(const float2* b, float2* v, int t) {
+  constexpr int NB = N / (R * T);
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    const int j = t + T * i;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int p = j + k * (N / R);
+      v[i * R + k] = b[p + (p >> SH)];
+    }
+  }
+}
+
+template <int N, int T, int NP, bool INV, int NS, int OFF, int R, int... Rest>
+__device__ __forceinline__ void run_wstages_impl(float2* v, float2* b, const float4* tw, int t) {
+  stage_compute<N, T, R, NS, INV, OFF>(v, tw, t);
+  if constexpr (sizeof...(Rest) > 0) {
+    constexpr int RN = First<Rest...>::value;
+    constexpr int SH = XPad<N, T, NP>::best(R, NS, RN);
+    __syncwarp();
+    wstage_write<N, T, R, NS, SH>(b, v, t);
+    __syncwarp();
+    wstage_read<N, T, RN, SH>(b, v, t);
+    run_wstages_impl<N, T, NP, INV, NS * R, OFF + NS * (R - 1), Rest...>(v, b, tw, t);
+  }
+}
+
+// tw: the stage-major table of this radix order; b: the group's buffer (NP words)
+template <int N, int T, int NP, bool INV, int... Rs>
+__device__ __forceinline__ void run_wstages(Radices<Rs...>, float2* v, float2* b, const float4* tw, int t) {
+  run_wstages_impl<N, T, NP, INV, 1, 0, Rs...>(v, b, tw, t);
+}
+
+// Register slot q = i R + k holds point slot_pos<R>(t, i, k) = t + T (i + k N/(R T)).
+// reorder<RA, RB>: registers positioned for radix RA -> positioned for RB
+// (the same set of points t + T m, only the slot order differs).
+template <int N, int T, int RA, int RB>
+__device__ __forceinline__ void reorder(const float2* a, float2* b) {
+  constexpr int MA = N / (RA * T), MB = N / (RB * T);
+#pragma unroll
+  for (int ib = 0; ib < MB; ++ib)
+#pragma unroll
+    for (int kb = 0; kb < RB; ++kb) {
+      const int m = ib + kb * MB;      // point t + T m
+      const int ia = m % MA, ka = m / MA;
+      b[ib * RB + kb] = a[ia * RA + ka];
+    }
+}
+
+// Plans of the x passes: lanes per line T (dividing 32) and radix order.  A
+// full warp per line where the radices allow it keeps the points per lane
+// (and so the registers) low.
+template <int N>
+struct XPlan : Plan<N> {};
+template <>
+struct XPlan<256> {
+  static constexpr int N = 256, T = 32;
+  using Fwd = Radices<8, 8, 4>;
+};
+template <>
+struct XPlan<384> {
+  static constexpr int N = 384, T = 32;
+  using Fwd = Radices<6, 4, 4, 4>;
+};
+
+template <int N>
+struct XCfg {
+  static constexpr int T = XPlan<N>::T;
+  static_assert(32 % T == 0, "x pass: threads per line must divide the warp");
+  static constexpr int GROUPS = 32 / T;                // row pairs per warp
+  static constexpr int WARPS = 4;                      // warps per CTA
+  static constexpr int NT = 32 * WARPS;
+  static constexpr int NP = N + N / 4 + 1;             // padded exchange buffer per group
+  static constexpr size_t SMEM = sizeof(float4) * 2 * N + sizeof(float2) * (size_t)NP * GROUPS * WARPS;
+};
+
+// Work distribution: warp-units of GROUPS row pairs, grid-stride over all
+// batch items; every lane of a warp runs the same number of iterations.
+struct XWork {
+  int pairs_per_item;   // nrows / 2
+  int batch;
+  __device__ __forceinline__ long long units(int groups) const {
+    return ((long long)pairs_per_item * batch + groups - 1) / groups;
+  }
+};
+
+// Packed potential line of rows (A, B) from their half spectra, loaded at the
+// register slots of radix R: Z[p] = A[p] + i B[p], Z[N-p] = conj A[p] + i conj B[p].
+template <int N, int T, int R>
+__device__ __forceinline__ void load_packed_half(float2* v, const float2* __restrict__ ha,
+                                                 const float2* __restrict__ hb, bool ok, int t) {
+#pragma unroll
+  for (int i = 0; i < N / (R * T); ++i)
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int p = slot_pos<N, T, R>(t, i, k);
+      const int q = p <= N / 2 ? p : N - p;
+      float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+      if (ok) {
+        a = ha[q];
+        b = hb[q];
+      }
+      v[i * R + k] = p <= N / 2 ? make_float2(a.x - b.y, a.y + b.x) : make_float2(a.x + b.y, b.x - a.y);
+    }
+}
+
+// Hermitian split of the packed forward transform (registers at radix-R slots)
+// into the half spectra of rows A and B (k = 0..N/2), via the group buffer.
+template <int N, int T, int R>
+__device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, float2* __restrict__ ha,
+                                                  float2* __restrict__ hb, bool ok, int t) {
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < N / (R * T); ++i)
+#pragma unroll
+    for (int k = 0; k < R; ++k) buf[slot_pos<N, T, R>(t, i, k)] = v[i * R + k];
+  __syncwarp();
+  if (!ok) return;
+#pragma unroll
+  for (int i = 0; i < N / (R * T); ++i)
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int p = slot_pos<N, T, R>(t, i, k);
+      if (p > N / 2) continue;
+      const float2 zk = v[i * R + k];
+      const float2 zn = buf[(N - p) % N];
+      ha[p] = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+      hb[p] = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+    }
+}
+
+#define WDM_XPASS_PROLOGUE                                                          \
+  using C = XCfg<N>;                                                                \
+  constexpr int T = C::T;                                                           \
+  using Rad = typename XPlan<N>::Fwd;                                               \
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;                  \
+  (void)R1;                                                                         \
+  (void)RS;                                                                         \
+  extern __shared__ float2 smem[];                                                  \
+  float4* tw = reinterpret_cast<float4*>(smem); /* [x fwd | x rev] tables */      \
+  const float4* twr = tw + N;                                                       \
+  (void)twr;                                                                        \
+  load_twiddles(tw, twg + TW_X_FWD * N, 2 * N);                                     \
+  __syncthreads();                                                                  \
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;                       \
+  const int g = lane / T, t = lane % T;                                             \
+  float2* buf = smem + 4 * N + (size_t)(warp * C::GROUPS + g) * C::NP;              \
+  const long long nunits = w.units(C::GROUPS);                                      \
+  const long long wstride = (long long)gridDim.x * C::WARPS;
+
+// ----------------------------------------------------------------------------
+// P1: Phi rows from H (C2R of the packed pair), kick, forward x-FFT (or not)
+// ----------------------------------------------------------------------------
+template <int N, bool FWD>
+__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+k_xw_kick(float2* __restrict__ psi, const float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
+          const float4* __restrict__ twg, KickArgs a, XWork w) {
+  WDM_XPASS_PROLOGUE
+  using Rev = typename Reverse<Rad>::type;
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+    const float2* hrow = H + b * hbstride + ra * hpitch;
+    float2 v[N / T];
+    load_packed_half<N, T, RadInfo<Rev>::first>(v, hrow, hrow + hpitch, ok, t);
+    run_wstages<N, T, C::NP, true>(Rev{}, v, buf, twr, t);  // ends with radix R1
+    float phi[2][N / T];
+#pragma unroll
+    for (int q = 0; q < N / T; ++q) {
+      phi[0][q] = v[q].x;
+      phi[1][q] = v[q].y;
+    }
+    float T6[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int r = ra + half;
+      float2* row = psi + b * rg.bstride + (long long)r * rg.pitch;
+      const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+      const int y = r % rg.ny, z = r / rg.ny;
+      const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * z;
+      // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2)
+      const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
+      const float lin = T6[3] * fy + T6[4] * fz;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) {
+          const int q = i * R1 + k;
+          const int x = slot_pos<N, T, R1>(t, i, k);
+          float pot = phi[half][q];
+          if (a.tidal) {
+            const float fx = a.x0 + a.dx * x;
+            pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
+          }
+          if (a.kerr != 0.f) pot += a.kerr * (v[q].x * v[q].x + v[q].y * v[q].y);
+          if (vrow && ok) pot += vrow[x];
+          v[q] = apply_kick(v[q], pot, a);
+        }
+      if constexpr (FWD) {
+        run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+        if (ok)
+#pragma unroll
+          for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+            for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+      } else {
+        if (ok)
+#pragma unroll
+          for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+            for (int k = 0; k < R1; ++k) row[slot_pos<N, T, R1>(t, i, k)] = v[i * R1 + k];
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// P5: psi x-inverse (+mask) of rows A and B, rho = |psi|^2 (+rho_b) - shift,
+// packed R2C of (rho_A, rho_B) -> H rows A and B
+// ----------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
+             const float4* __restrict__ twg, RhoArgs a, XWork w) {
+  WDM_XPASS_PROLOGUE
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+    const float shift = a.shift ? a.shift[b] : 0.f;
+    float rho0[N / T];  // row A density at radix-RS slots
+    float2 z[N / T];    // packed (rho_A, rho_B) at radix-RS slots
+    float2 v[N / T];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int r = ra + half;
+      float2* row = psi + b * rg.bstride + (long long)r * rg.pitch;
+      if (a.write_psi) {
+#pragma unroll
+        for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+          for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+        run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
+        if (a.mx) {
+          const int y = r % rg.ny, z = r / rg.ny;
+          const float myz = ok ? a.my[y] * a.mz[z] : 0.f;
+#pragma unroll
+          for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+            for (int k = 0; k < RS; ++k)
+              v[i * RS + k] = cscale(v[i * RS + k], myz * a.mx[slot_pos<N, T, RS>(t, i, k)]);
+        }
+        if (ok)
+#pragma unroll
+          for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+            for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+      } else {
+#pragma unroll
+        for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+          for (int k = 0; k < RS; ++k) v[i * RS + k] = ok ? row[slot_pos<N, T, RS>(t, i, k)] : make_float2(0.f, 0.f);
+      }
+      const float* rb = a.rho_b ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) {
+          const float2 q = v[i * RS + k];
+          float d = q.x * q.x + q.y * q.y;
+          if (a.nonfinite && !isfinite(d)) *a.nonfinite = 1;
+          if (rb && ok) d += rb[slot_pos<N, T, RS>(t, i, k)];
+          if (half == 0) rho0[i * RS + k] = d - shift;
+          else z[i * RS + k] = make_float2(rho0[i * RS + k], d - shift);
+        }
+    }
+    reorder<N, T, RS, R1>(z, v);
+    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+    float2* hrow = H + b * hbstride + ra * hpitch;
+    store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, ok, t);
+  }
+}
+
+// Plain C2C x pass (rows processed pairwise, scaled output).
+template <int N, bool INV>
+__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+k_xw_fft(float2* __restrict__ data, RowGeom rg, const float4* __restrict__ twg, float scale, XWork w) {
+  WDM_XPASS_PROLOGUE
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float2* row = data + b * rg.bstride + (long long)(ra + half) * rg.pitch;
+      float2 v[N / T];
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+      run_wstages<N, T, C::NP, INV>(Rad{}, v, buf, tw, t);
+      if (ok)
+#pragma unroll
+        for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+          for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = cscale(v[i * RS + k], scale);
+    }
+  }
+}
+
+// Phi rows (real) from H: packed C2R only.
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+k_xw_c2r(const float2* __restrict__ H, float* __restrict__ out, RowGeom rg, long long hpitch, long long hbstride,
+         const float4* __restrict__ twg, XWork w) {
+  WDM_XPASS_PROLOGUE
+  using Rev = typename Reverse<Rad>::type;
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+    const float2* hrow = H + b * hbstride + ra * hpitch;
+    float2 v[N / T];
+    load_packed_half<N, T, RadInfo<Rev>::first>(v, hrow, hrow + hpitch, ok, t);
+    run_wstages<N, T, C::NP, true>(Rev{}, v, buf, twr, t);
+    if (!ok) continue;
+    float* oa = out + b * rg.bstride + (long long)ra * rg.pitch;
+#pragma unroll
+    for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+      for (int k = 0; k < R1; ++k) {
+        const int x = slot_pos<N, T, R1>(t, i, k);
+        oa[x] = v[i * R1 + k].x;
+        oa[rg.pitch + x] = v[i * R1 + k].y;
+      }
+  }
+}
+
+// Real rows -> H (packed R2C) from a float field, minus a per-item shift.
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+k_xw_r2c(const float* __restrict__ in, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
+         const float4* __restrict__ twg, const float* __restrict__ shift_b, XWork w) {
+  WDM_XPASS_PROLOGUE
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+    const float shift = shift_b ? shift_b[b] : 0.f;
+    const float* ia = in + b * rg.bstride + (long long)ra * rg.pitch;
+    float2 v[N / T];
+#pragma unroll
+    for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+      for (int k = 0; k < R1; ++k) {
+        const int x = slot_pos<N, T, R1>(t, i, k);
+        v[i * R1 + k] = ok ? make_float2(ia[x] - shift, ia[rg.pitch + x] - shift) : make_float2(0.f, 0.f);
+      }
+    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+    float2* hrow = H + b * hbstride + ra * hpitch;
+    store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, ok, t);
+  }
+}
+
+#undef WDM_XPASS_PROLOGUE
+
+}  // namespace wdm
