@@ -115,6 +115,24 @@ wdm_status wdm_drift(wdm_ctx* ctx, double dt);
 wdm_status wdm_poisson(wdm_ctx* ctx, const float* rho, float* phi, int32_t where);
 /* in-place 3D C2C FFT of a complex64 device array (dir = -1 forward, +1 inverse, unnormalised) */
 wdm_status wdm_fft3d(wdm_ctx* ctx, void* data_dev, int32_t dir);
+/* The same Poisson solve as wdm_poisson for one device-resident grid, for callers
+ * that cannot allocate device memory: code running under a host runtime that owns
+ * the GPU's memory pool and allows no allocation outside it (for example a Julia
+ * CUDA.jl process with a memory limit), or a time-critical loop in which the
+ * implicit device synchronisation of cudaMalloc/cudaFree would stall other work.
+ * It needs no context and calls no cudaMalloc, cudaFree or other allocating
+ * routine.  Its scratch is one static device array of about 8.3 MiB that every
+ * GPU loading the library holds until the process exits; grids are limited to
+ * (nx/2+1)*ny*nz <= 1,064,960 (a 128^3 grid), larger ones return
+ * WDM_ERR_INVALID.  rho and phi are float32 device pointers [nz][ny][nx]; stream is
+ * a cudaStream_t (NULL: the default stream); the call returns when phi is ready.
+ * The first call on a device looks up the array's device address once, so make
+ * that first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU race and must be serialised by the caller.
+ * Errors are reported through wdm_last_error(NULL).
+ * No counterpart in the reference: it is an addition of this library. */
+wdm_status wdm_poisson_noalloc(const float* rho_dev, float* phi_dev, int32_t nx, int32_t ny, int32_t nz,
+                               double lx, double ly, double lz, double poisson_coeff, void* stream);
 
 /* diagnostics --------------------------------------------------------------- */
 /* out[0..9] (per batch item, 10 doubles each): mass, rho_max, argmax (flat index),

@@ -63,6 +63,7 @@ SIGNATURES = [
     ("wdm_drift", _i32, [_vp, _d]),
     ("wdm_poisson", _i32, [_vp, _vp, _vp, _i32]),
     ("wdm_fft3d", _i32, [_vp, _vp, _i32]),
+    ("wdm_poisson_noalloc", _i32, [_vp, _vp, _i32, _i32, _i32, _d, _d, _d, _d, _vp]),
     ("wdm_reduce", _i32, [_vp, _vp]),
     ("wdm_interpolate_phi", _i32, [_vp, _vp, _i64, _vp]),
     ("wdm_check_finite", _i32, [_vp, C.POINTER(_i32)]),

@@ -51,6 +51,9 @@ using namespace wdm;
 
 static std::string g_create_error;
 
+// Message returned by wdm_last_error(NULL) for entry points without a context.
+void wdm_set_global_error(const std::string& msg) { g_create_error = msg; }
+
 // Passes of the pipeline, for launch counting and per-pass event timing.
 enum Pass {
   P_KICK_FWD = 0,  // P1: Phi C2R + kick + psi x-FFT
