@@ -106,6 +106,22 @@ wdm_status wdm_set_particles(wdm_ctx* ctx, const double* pos, const double* mass
 /* nsteps steps of size dt from time t0 */
 wdm_status wdm_step(wdm_ctx* ctx, int32_t nsteps, double dt, double t0, int32_t mode);
 wdm_status wdm_step_async(wdm_ctx* ctx, int32_t nsteps, double dt, double t0, int32_t mode);
+/* wdm_step through a CUDA graph: the launches of nsteps steps are captured once
+ * per (nsteps, dt, mode, state) and replayed; returns when the steps are done. */
+wdm_status wdm_step_graph(wdm_ctx* ctx, int32_t nsteps, double dt, int32_t mode);
+
+/* ensembles: contexts of different grid sizes (each holding `batch` halos of
+ * its size) advanced together; their steps are captured into one CUDA graph on
+ * one stream and replayed as a single graph launch per call.  Member contexts
+ * stay owned by the caller and must outlive the group. */
+typedef struct wdm_group wdm_group;
+wdm_status wdm_group_create(wdm_ctx* const* members, int32_t n, wdm_group** out);
+wdm_status wdm_group_destroy(wdm_group* g);
+/* nsteps steps of every member, member i with time step dts[i] */
+wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode);
+/* kernel launches executed by the group's graph replays so far */
+int64_t wdm_group_launch_count(const wdm_group* g);
+
 /* apply_kick_step!: Phi from |psi|^2, psi <- exp(-i dt (Phi + V + tide(t))) psi */
 wdm_status wdm_kick(wdm_ctx* ctx, double dt, double t);
 /* apply_drift_step!: psi <- mask * ifft(exp(-i k^2 dt/2) fft(psi)) */
@@ -158,6 +174,11 @@ int32_t wdm_num_passes(void);
 const char* wdm_pass_name(int32_t p);
 /* kernel launches issued by this context since creation */
 int64_t wdm_launch_count(const wdm_ctx* ctx);
+
+/* self-test ------------------------------------------------------------------ */
+/* out[2i], out[2i+1] = sin, cos of h[i] (|h| <= pi/2) as evaluated by the series
+ * the precise phase form uses; device pointers, n values. */
+wdm_status wdm_selftest_sincos(const float* h_dev, float* out_dev, int64_t n);
 
 #ifdef __cplusplus
 }

@@ -233,3 +233,25 @@ def test_nonfinite_is_reported(wdm):
             ctx.step(1, 0.01)
         assert ei.value.status == 5
         assert not ctx.is_finite()
+
+
+def test_series_sincos_error_bound(wdm, torch_cuda):
+    """The precise phase form's branch-free sin/cos of |h| <= pi/2 stays within 2 ulp of FP64."""
+    import ctypes as C
+
+    torch = torch_cuda
+    h = np.linspace(-np.pi / 2, np.pi / 2, 200001).astype(np.float32)
+    hd = torch.from_numpy(h).cuda()
+    out = torch.empty(2 * h.size, dtype=torch.float32, device="cuda")
+    assert wdm._abi.load().wdm_selftest_sincos(C.c_void_p(hd.data_ptr()), C.c_void_p(out.data_ptr()), h.size) == 0
+    sc = out.cpu().numpy().reshape(-1, 2).astype(np.float64)
+    s_ref, c_ref = np.sin(h.astype(np.float64)), np.cos(h.astype(np.float64))
+    ulp_s = np.spacing(np.abs(s_ref).astype(np.float32)).astype(np.float64)
+    ulp_c = np.spacing(np.abs(c_ref).astype(np.float32)).astype(np.float64)
+    assert np.max(np.abs(sc[:, 0] - s_ref) / np.maximum(ulp_s, 1e-45)) <= 2.0
+    # cos = 1 - h^2/2 + ... sums terms of order 1, so it is accurate to 1 ulp of
+    # 1 absolutely (what a phase factor needs) and to 2 ulp relatively only
+    # where |cos| stays near 1
+    assert np.max(np.abs(sc[:, 1] - c_ref)) <= 1.2e-7
+    near1 = np.abs(c_ref) >= 0.7
+    assert np.max(np.abs(sc[near1, 1] - c_ref[near1]) / ulp_c[near1]) <= 2.0

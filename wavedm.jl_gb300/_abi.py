@@ -1,7 +1,8 @@
 """ctypes binding of libwavedm (the C ABI declared in include/wavedm.h).
 
-The library is built in-tree (``wavedm.jl_gb300/libwavedm.so``).  Loading it
-never falls back to anything else: a missing or unloadable library raises.
+The library is built in-tree (``wavedm.jl_gb300/libwavedm.so``; the environment
+variable WDM_LIB_PATH selects another build).  Loading it never falls back to
+anything else: a missing or unloadable library raises.
 """
 from __future__ import annotations
 
@@ -73,6 +74,12 @@ SIGNATURES = [
     ("wdm_num_passes", _i32, []),
     ("wdm_pass_name", C.c_char_p, [_i32]),
     ("wdm_launch_count", _i64, [_vp]),
+    ("wdm_selftest_sincos", _i32, [_vp, _vp, _i64]),
+    ("wdm_step_graph", _i32, [_vp, _i32, _d, _i32]),
+    ("wdm_group_create", _i32, [_vp, _i32, C.POINTER(_vp)]),
+    ("wdm_group_destroy", _i32, [_vp]),
+    ("wdm_group_step", _i32, [_vp, _i32, _vp, _i32]),
+    ("wdm_group_launch_count", _i64, [_vp]),
 ]
 
 _lib = None
@@ -91,7 +98,7 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("WDM_LIB_PATH") or LIB_PATH
     if not os.path.exists(p):
         raise ImportError(
             f"libwavedm.so not found at {p}: build it with `python wavedm.jl_gb300/build.py` "

@@ -53,8 +53,8 @@ def needs_build():
     return _newest(sources() + headers()) > os.path.getmtime(LIB)
 
 
-def _compile(src, verbose=False, extra=()):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src, verbose=False, extra=(), build_dir=BUILD):
+    obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -64,28 +64,36 @@ def _compile(src, verbose=False, extra=()):
     return obj
 
 
-def build(force=False, verbose=False, ptxas_info=False):
-    """Compile every csrc/*.cu for sm_103a and link libwavedm.so; returns its path."""
-    if not force and not needs_build():
+def build(force=False, verbose=False, ptxas_info=False, defines=(), out=None):
+    """Compile every csrc/*.cu for sm_103a and link libwavedm.so; returns its path.
+
+    ``defines`` (e.g. ["WDM_X_MINB=6"]) and ``out`` build a tuning variant of
+    the library at another path, with objects in a directory beside it.
+    """
+    lib = os.path.abspath(out) if out else LIB
+    if not force and not defines and out is None and not needs_build():
         return LIB
-    os.makedirs(BUILD, exist_ok=True)
-    extra = ("-Xptxas", "-v") if ptxas_info else ()
+    build_dir = BUILD if out is None else lib + ".objs"
+    os.makedirs(build_dir, exist_ok=True)
+    extra = tuple(("-Xptxas", "-v") if ptxas_info else ()) + tuple("-D" + d for d in defines)
     srcs = sources()
     workers = min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(workers) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose or ptxas_info, extra), srcs))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, verbose or ptxas_info, extra, build_dir), srcs))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--ptxas-info", action="store_true", help="print registers/spills per kernel")
+    ap.add_argument("--define", "-D", action="append", default=[], help="extra preprocessor define (variant build)")
+    ap.add_argument("--out", default=None, help="output path of a variant library")
     a = ap.parse_args()
-    print(build(force=a.force or a.ptxas_info, verbose=True, ptxas_info=a.ptxas_info))
+    print(build(force=a.force or a.ptxas_info, verbose=True, ptxas_info=a.ptxas_info, defines=a.define, out=a.out))

@@ -139,6 +139,10 @@ class SPEContext:
         fn = self.lib.wdm_step if sync else self.lib.wdm_step_async
         self._check(fn(self.handle, int(nsteps), float(dt), float(t0), _abi.STEP_MODES[mode]))
 
+    def step_graph(self, nsteps, dt, mode="strang"):
+        """Same as step(), replayed from a captured CUDA graph."""
+        self._check(self.lib.wdm_step_graph(self.handle, int(nsteps), float(dt), _abi.STEP_MODES[mode]))
+
     def kick(self, dt, t=0.0):
         self._check(self.lib.wdm_kick(self.handle, float(dt), float(t)))
 
@@ -207,6 +211,48 @@ class SPEContext:
     @property
     def launch_count(self):
         return int(self.lib.wdm_launch_count(self.handle))
+
+
+class Ensemble:
+    """Independent halos of several grid sizes advanced together.
+
+    ``members`` are SPEContexts (one per grid size, each with ``batch`` halos);
+    every call to step() runs all their steps from one captured CUDA graph
+    (wdm_group_step).  The contexts stay owned by the caller.
+    """
+
+    def __init__(self, members):
+        self.lib = _abi.load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.handle.value for m in self.members])
+        h = C.c_void_p()
+        check(self.lib.wdm_group_create(arr, len(self.members), C.byref(h)))
+        self._h = h
+
+    def step(self, nsteps, dts, mode="strang"):
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dts, np.float64), (len(self.members),)))
+        check(self.lib.wdm_group_step(self._h, int(nsteps), C.c_void_p(d.ctypes.data), _abi.STEP_MODES[mode]))
+
+    @property
+    def launch_count(self):
+        return int(self.lib.wdm_group_launch_count(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.wdm_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def size_supported(n):

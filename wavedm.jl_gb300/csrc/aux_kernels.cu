@@ -1,7 +1,24 @@
 // Auxiliary kernels: density output, FP64 diagnostics reductions, CIC.
 #include "aux_kernels.cuh"
+#include "wdm_math.cuh"
 
 namespace wdm {
+
+__global__ void k_sincos_half(const float* __restrict__ h, float* __restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float s, c;
+    sincos_half(h[i], &s, &c);
+    out[2 * i] = s;
+    out[2 * i + 1] = c;
+  }
+}
+
+cudaError_t launch_sincos_half(const float* h, float* out, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const long long b = (n + 255) / 256;
+  k_sincos_half<<<(unsigned)(b < 4096 ? b : 4096), 256, 0, st>>>(h, out, n);
+  return cudaGetLastError();
+}
 
 __global__ void k_abs2(const float2* __restrict__ psi, float* __restrict__ out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {

@@ -32,6 +32,8 @@ struct RedGeom {
 };
 
 cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t st);
+// out[2i], out[2i+1] = series sin, cos of h[i] (wdm_math.cuh), for self-tests
+cudaError_t launch_sincos_half(const float* h, float* out, long long n, cudaStream_t st);
 // shift[b] = mean over item b of |data|^2 (complex_in) or of data (float), + add
 cudaError_t launch_mean_shift(const void* data, bool complex_in, long long n, int batch, double* sums, float* shift,
                               double add, cudaStream_t st);

@@ -177,8 +177,13 @@ WDM_PLAN(64, 8, 8, 8)
 WDM_PLAN(96, 8, 4, 4, 6)
 WDM_PLAN(128, 16, 8, 4, 4)
 WDM_PLAN(192, 16, 4, 4, 4, 3)
+#if defined(WDM_LINE_PLAN_T32)
+WDM_PLAN(256, 32, 8, 8, 4)
+WDM_PLAN(384, 32, 6, 4, 4, 4)
+#else
 WDM_PLAN(256, 16, 8, 8, 4)
 WDM_PLAN(384, 16, 8, 8, 6)
+#endif
 WDM_PLAN(512, 32, 8, 8, 8)
 #undef WDM_PLAN
 

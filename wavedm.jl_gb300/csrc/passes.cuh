@@ -16,6 +16,7 @@
 //   P8 k_lfft<inv>    H, y axis
 #pragma once
 #include "fft_engine.cuh"
+#include "wdm_math.cuh"
 
 namespace wdm {
 
@@ -26,7 +27,13 @@ template <int N>
 __host__ __device__ constexpr int threads_for() { return Plan<N>::T * LINES; }
 
 template <int N>
-__host__ __device__ constexpr int min_blocks() { return threads_for<N>() >= 512 ? 1 : 512 / threads_for<N>(); }
+__host__ __device__ constexpr int min_blocks() {
+#ifdef WDM_LINE_THREADS_PER_SM
+  return threads_for<N>() >= WDM_LINE_THREADS_PER_SM ? 1 : WDM_LINE_THREADS_PER_SM / threads_for<N>();
+#else
+  return threads_for<N>() >= 512 ? 1 : 512 / threads_for<N>();
+#endif
+}
 
 template <int N>
 __host__ __device__ constexpr size_t smem_bytes() { return sizeof(float2) * (size_t)(2 * N + N * LPITCH); }
@@ -98,9 +105,7 @@ struct DriftOp {
       const float lo = ((e1 + e2) + (tx.y + ty.y)) + tz.y;
       const float n = rintf(s2 * 0.15915494309189535f);
       const float r = fmaf(-n, 6.28318548202514648f, s2) + fmaf(-n, -1.7484555e-07f, lo);
-      float sn, cs;
-      sincosf(0.5f * r, &sn, &cs);
-      const float2 em1 = make_float2(-2.f * sn * sn, -2.f * sn * cs);  // exp(-i r) - 1
+      const float2 em1 = expm1_neg_i(r);  // exp(-i r) - 1
       const float2 w = cadd(v, cmul(v, em1));
       return make_float2(fmaf(w.x, scale, w.x * scale_lo), fmaf(w.y, scale, w.y * scale_lo));
     }
@@ -237,9 +242,9 @@ struct KickArgs {
 // Plain form: one FP32 sincos of pot*dt.
 // Precise form: theta = pot*dt as an unevaluated float pair, reduced by 2 pi
 // (Cody-Waite with a two-term 2 pi) to |r| <= pi, then applied as
-// psi + psi (exp(-i r) - 1) with exp(-i r) - 1 = (-2 sin^2(r/2), -sin r) from one
-// sincos of r/2: accurate relative to |exp(-i r) - 1|, so small kicks do not
-// carry the fixed modulus error of an FP32 cosine rounded near 1.
+// psi + psi (exp(-i r) - 1) with exp(-i r) - 1 = (-2 sin^2(r/2), -sin r) from the
+// series sin/cos of r/2 (wdm_math.cuh): accurate relative to |exp(-i r) - 1|, so
+// small kicks do not carry the fixed modulus error of a cosine rounded near 1.
 __device__ __forceinline__ float2 apply_kick(float2 v, float pot, const KickArgs& a) {
   float s, c;
   if (a.precise) {
@@ -247,10 +252,8 @@ __device__ __forceinline__ float2 apply_kick(float2 v, float pot, const KickArgs
     const float te = fmaf(pot, a.dt_hi, -th) + pot * a.dt_lo;
     const float n = rintf(th * 0.15915494309189535f);
     const float r = fmaf(-n, 6.28318548202514648f, th) + fmaf(-n, -1.7484555e-07f, te);
-    sincosf(0.5f * r, &s, &c);
-    const float em1_re = -2.f * s * s;  // cos r - 1
-    const float em1_im = -2.f * s * c;  // -sin r
-    return make_float2(v.x + (v.x * em1_re - v.y * em1_im), v.y + (v.x * em1_im + v.y * em1_re));
+    const float2 e = expm1_neg_i(r);  // (cos r - 1, -sin r)
+    return make_float2(v.x + (v.x * e.x - v.y * e.y), v.y + (v.x * e.y + v.y * e.x));
   }
   sincosf(pot * a.dt_hi, &s, &c);
   return cmul(v, make_float2(c, -s));

@@ -124,6 +124,8 @@ struct wdm_ctx {
   int have_psi = 0;
   int phi_valid = 0;
   int64_t launch_count = 0;
+  long long version = 0;            // bumped by every set_* call that a captured graph bakes in
+  struct wdm_group* self_group = nullptr;  // single-member group of wdm_step_graph
   Profiler prof;
   std::string err;
 };
@@ -542,6 +544,7 @@ void* wdm_stream(wdm_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
 
 wdm_status wdm_destroy(wdm_ctx* c) {
   if (!c) return WDM_OK;
+  if (c->self_group) wdm_group_destroy(c->self_group);
   if (c->st) cudaStreamSynchronize(c->st);
   void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
                   c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->parts, c->T6b, c->flag, c->scratch_f,
@@ -676,6 +679,7 @@ wdm_status wdm_get_phi(wdm_ctx* c, float* phi, int32_t where) {
 
 wdm_status wdm_set_static_potential(wdm_ctx* c, const float* V, int32_t where) {
   if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  c->version++;
   if (!V) {
     if (c->V) cudaFree(c->V);
     c->V = nullptr;
@@ -689,6 +693,7 @@ wdm_status wdm_set_static_potential(wdm_ctx* c, const float* V, int32_t where) {
 
 wdm_status wdm_set_tidal(wdm_ctx* c, const double* sched, int32_t nsched, int32_t per_item) {
   if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  c->version++;
   if (nsched < 0) return fail(c, WDM_ERR_INVALID, "nsched < 0");
   if (nsched == 0) {
     c->tide_on = 0;
@@ -713,6 +718,7 @@ wdm_status wdm_set_tidal(wdm_ctx* c, const double* sched, int32_t nsched, int32_
 
 wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, int64_t n) {
   if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  c->version++;
   if (n < 0) return fail(c, WDM_ERR_INVALID, "n < 0");
   if (n > 0 && c->d.batch != 1) return fail(c, WDM_ERR_UNSUPPORTED, "baryon particles need batch == 1");
   if (c->parts) cudaFree(c->parts);
@@ -953,6 +959,14 @@ wdm_status wdm_interpolate_phi(wdm_ctx* c, const double* pos, int64_t n, double*
   return WDM_OK;
 }
 
+wdm_status wdm_selftest_sincos(const float* h, float* out, int64_t n) {
+  if (!h || !out || n < 0) return fail(nullptr, WDM_ERR_INVALID, "wdm_selftest_sincos: bad arguments");
+  cudaError_t e = launch_sincos_half(h, out, n, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return fail(nullptr, WDM_ERR_CUDA, std::string("wdm_selftest_sincos: ") + cudaGetErrorString(e));
+  return WDM_OK;
+}
+
 int32_t wdm_num_passes(void) { return NPASS; }
 
 const char* wdm_pass_name(int32_t p) { return (p >= 0 && p < NPASS) ? PASS_NAMES[p] : ""; }
@@ -989,6 +1003,143 @@ wdm_status wdm_check_finite(wdm_ctx* c, int32_t* finite) {
   WDM_CU(c, cudaMemcpy(&flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost));
   if (fault_injected("nonfinite")) flag = 1;
   *finite = flag ? 0 : 1;
+  return WDM_OK;
+}
+
+// --------------------------------------------------------------------------
+// CUDA-graph replay of whole step sequences, for one context or an ensemble
+// --------------------------------------------------------------------------
+struct wdm_group {
+  std::vector<wdm_ctx*> m;
+  cudaStream_t st = nullptr;
+  struct Entry {
+    int nsteps, mode;
+    std::vector<double> dts;
+    std::vector<long long> versions;
+    cudaGraphExec_t exec;
+    int64_t launches;
+  };
+  std::vector<Entry> cache;
+  int64_t launches = 0;
+};
+
+// Everything a captured step sequence must not do inside the capture (table
+// uploads with a host sync, the first potential) is done here, eagerly.
+static wdm_status prepare_capture(wdm_ctx* c, double dt) {
+  WDM_TRY(need_psi(c));
+  if (c->d.phase_mode == WDM_PHASE_PRECISE) WDM_TRY(ensure_drift_tables(c, dt));
+  if (c->d.absorb_alpha != 0.0) WDM_TRY(ensure_mask_tables(c, dt));
+  if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  return WDM_OK;
+}
+
+static wdm_status group_fail(wdm_status s, const std::string& msg) { return fail(nullptr, s, msg); }
+
+wdm_status wdm_group_create(wdm_ctx* const* members, int32_t n, wdm_group** out) {
+  if (!members || n <= 0 || !out) return group_fail(WDM_ERR_INVALID, "wdm_group_create: bad arguments");
+  *out = nullptr;
+  wdm_group* g = new wdm_group();
+  for (int i = 0; i < n; ++i) {
+    if (!members[i]) {
+      delete g;
+      return group_fail(WDM_ERR_INVALID, "wdm_group_create: null member");
+    }
+    g->m.push_back(members[i]);
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete g;
+    return group_fail(WDM_ERR_CUDA, std::string("wdm_group_create: ") + cudaGetErrorString(e));
+  }
+  *out = g;
+  return WDM_OK;
+}
+
+wdm_status wdm_group_destroy(wdm_group* g) {
+  if (!g) return WDM_OK;
+  if (g->st) cudaStreamSynchronize(g->st);
+  for (auto& en : g->cache) cudaGraphExecDestroy(en.exec);
+  if (g->st) cudaStreamDestroy(g->st);
+  delete g;
+  return WDM_OK;
+}
+
+int64_t wdm_group_launch_count(const wdm_group* g) { return g ? g->launches : 0; }
+
+wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode) {
+  if (!g || !dts || nsteps < 0) return group_fail(WDM_ERR_INVALID, "wdm_group_step: bad arguments");
+  if (nsteps == 0) return WDM_OK;
+  const size_t n = g->m.size();
+  std::vector<double> dt(dts, dts + n);
+  std::vector<long long> ver(n);
+  for (size_t i = 0; i < n; ++i) {
+    wdm_status s = prepare_capture(g->m[i], dt[i]);
+    if (s != WDM_OK) return group_fail(s, "wdm_group_step: member " + std::to_string(i) + ": " + g->m[i]->err);
+    ver[i] = g->m[i]->version;
+  }
+  wdm_group::Entry* hit = nullptr;
+  for (auto& en : g->cache)
+    if (en.nsteps == nsteps && en.mode == mode && en.dts == dt && en.versions == ver) hit = &en;
+  if (!hit) {
+    if (g->cache.size() >= 8) {
+      cudaGraphExecDestroy(g->cache.front().exec);
+      g->cache.erase(g->cache.begin());
+    }
+    cudaError_t e = cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
+    int64_t launches = 0;
+    wdm_status bad = WDM_OK;
+    std::string why;
+    for (size_t i = 0; i < n && bad == WDM_OK; ++i) {
+      wdm_ctx* c = g->m[i];
+      cudaStream_t own = c->st;
+      const bool prof = c->prof.on;
+      const int64_t l0 = c->launch_count;
+      c->st = g->st;
+      c->prof.on = false;
+      bad = step_impl(c, nsteps, dt[i], 0.0, mode);
+      if (bad != WDM_OK) why = c->err;
+      launches += c->launch_count - l0;
+      c->launch_count = l0;  // counted when the graph runs
+      c->st = own;
+      c->prof.on = prof;
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(g->st, &graph);
+    if (bad != WDM_OK || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      if (bad != WDM_OK) return group_fail(bad, "wdm_group_step: capture: " + why);
+      return group_fail(WDM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    g->cache.push_back({nsteps, mode, dt, ver, exec, launches});
+    hit = &g->cache.back();
+  }
+  cudaError_t e = cudaGraphLaunch(hit->exec, g->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->st);
+  if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  g->launches += hit->launches;
+  for (size_t i = 0; i < n; ++i) {
+    g->m[i]->launch_count += hit->launches / (int64_t)n;
+    wdm_status s = sync_and_check(g->m[i]);
+    if (s != WDM_OK) return group_fail(s, "wdm_group_step: member " + std::to_string(i) + ": " + g->m[i]->err);
+  }
+  return WDM_OK;
+}
+
+wdm_status wdm_step_graph(wdm_ctx* c, int32_t nsteps, double dt, int32_t mode) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (!c->self_group) {
+    wdm_ctx* self = c;
+    wdm_status s = wdm_group_create(&self, 1, &c->self_group);
+    if (s != WDM_OK) return fail(c, s, wdm_last_error(nullptr));
+  }
+  wdm_status s = wdm_group_step(c->self_group, nsteps, &dt, mode);
+  if (s != WDM_OK) return fail(c, s, wdm_last_error(nullptr));
   return WDM_OK;
 }
 

@@ -11,6 +11,12 @@
 #pragma once
 #include "passes.cuh"
 
+// resident CTAs per SM the x passes are compiled for (registers per thread
+// = 65536 / (128 threads x WDM_X_MINB))
+#ifndef WDM_X_MINB
+#define WDM_X_MINB 4
+#endif
+
 namespace wdm {
 
 // Exchange buffer addressing: point p of a group lives at word base + p +
@@ -245,7 +251,7 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
 // P1: Phi rows from H (C2R of the packed pair), kick, forward x-FFT (or not)
 // ----------------------------------------------------------------------------
 template <int N, bool FWD>
-__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_kick(float2* __restrict__ psi, const float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
           const float4* __restrict__ twg, KickArgs a, XWork w) {
   WDM_XPASS_PROLOGUE
@@ -320,7 +326,7 @@ k_xw_kick(float2* __restrict__ psi, const float2* __restrict__ H, RowGeom rg, lo
 // packed R2C of (rho_A, rho_B) -> H rows A and B
 // ----------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
              const float4* __restrict__ twg, RhoArgs a, XWork w) {
   WDM_XPASS_PROLOGUE
@@ -385,7 +391,7 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
 
 // Plain C2C x pass (rows processed pairwise, scaled output).
 template <int N, bool INV>
-__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_fft(float2* __restrict__ data, RowGeom rg, const float4* __restrict__ twg, float scale, XWork w) {
   WDM_XPASS_PROLOGUE
   for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
@@ -413,7 +419,7 @@ k_xw_fft(float2* __restrict__ data, RowGeom rg, const float4* __restrict__ twg, 
 
 // Phi rows (real) from H: packed C2R only.
 template <int N>
-__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_c2r(const float2* __restrict__ H, float* __restrict__ out, RowGeom rg, long long hpitch, long long hbstride,
          const float4* __restrict__ twg, XWork w) {
   WDM_XPASS_PROLOGUE
@@ -442,7 +448,7 @@ k_xw_c2r(const float2* __restrict__ H, float* __restrict__ out, RowGeom rg, long
 
 // Real rows -> H (packed R2C) from a float field, minus a per-item shift.
 template <int N>
-__global__ void __launch_bounds__(XCfg<N>::NT, 4)
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_r2c(const float* __restrict__ in, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
          const float4* __restrict__ twg, const float* __restrict__ shift_b, XWork w) {
   WDM_XPASS_PROLOGUE
