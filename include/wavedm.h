@@ -150,6 +150,23 @@ wdm_status wdm_fft3d(wdm_ctx* ctx, void* data_dev, int32_t dir);
 wdm_status wdm_poisson_noalloc(const float* rho_dev, float* phi_dev, int32_t nx, int32_t ny, int32_t nz,
                                double lx, double ly, double lz, double poisson_coeff, void* stream);
 
+/* differentiation ------------------------------------------------------------ */
+/* Adjoint of nsteps Strang steps from the context's psi_0 (left unchanged) for
+ * L = sum (|psi_N|^2 - rho_target)^2 dV per batch item.  Outputs:
+ *   grad       complex64 [batch][nz][ny][nx]: dL/dRe psi_0 + i dL/dIm psi_0
+ *   loss       L per batch item (doubles)
+ *   dloss_damp dL/da per batch item when tidal_dir (6 doubles) is given, for a
+ *              tide equal to a * tidal_dir (as set with wdm_set_tidal); may be NULL
+ * psi is checkpointed every ckpt_every steps and recomputed between checkpoints
+ * (memory: (nsteps/ckpt_every + ckpt_every + 2) copies of psi and its half
+ * spectrum).  rho_target is float32 on host or device (where_target); grad is
+ * written to host or device memory (where_grad).  No counterpart in the
+ * reference (it has no differentiation); the gradient is exact for the
+ * discrete run, FP32 rounding aside. */
+wdm_status wdm_adjoint(wdm_ctx* ctx, int32_t nsteps, double dt, int32_t ckpt_every, const float* rho_target,
+                       int32_t where_target, const double* tidal_dir, void* grad, int32_t where_grad, double* loss,
+                       double* dloss_damp);
+
 /* diagnostics --------------------------------------------------------------- */
 /* out[0..9] (per batch item, 10 doubles each): mass, rho_max, argmax (flat index),
  * centre of mass x, y, z, and the virial sums VirialPotential, TotalKineticE,

@@ -76,6 +76,7 @@ SIGNATURES = [
     ("wdm_launch_count", _i64, [_vp]),
     ("wdm_selftest_sincos", _i32, [_vp, _vp, _i64]),
     ("wdm_step_graph", _i32, [_vp, _i32, _d, _i32]),
+    ("wdm_adjoint", _i32, [_vp, _i32, _d, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
     ("wdm_group_create", _i32, [_vp, _i32, C.POINTER(_vp)]),
     ("wdm_group_destroy", _i32, [_vp]),
     ("wdm_group_step", _i32, [_vp, _i32, _vp, _i32]),

@@ -143,6 +143,27 @@ class SPEContext:
         """Same as step(), replayed from a captured CUDA graph."""
         self._check(self.lib.wdm_step_graph(self.handle, int(nsteps), float(dt), _abi.STEP_MODES[mode]))
 
+    def adjoint(self, nsteps, dt, rho_target, ckpt_every=20, tidal_dir=None, grad_out=None):
+        """Loss, gradient and tidal-amplitude derivative of L = sum(|psi_N|^2 - rho_target)^2 dV.
+
+        Returns (loss, grad, dL/da): grad = dL/dRe psi_0 + i dL/dIm psi_0 (complex64, the
+        context's layout); dL/da is None without ``tidal_dir``.  psi is left at psi_0.
+        """
+        if not _is_device(rho_target):
+            rho_target = np.ascontiguousarray(rho_target, dtype=np.float32)
+        if grad_out is None:
+            grad_out = np.empty(self.shape, np.complex64)
+        pt, wt = _ptr(rho_target)
+        pg, wg = _ptr(grad_out)
+        loss = np.zeros(self.batch, np.float64)
+        damp = np.zeros(self.batch, np.float64)
+        d6 = None if tidal_dir is None else np.ascontiguousarray(np.asarray(tidal_dir, np.float64).reshape(6))
+        self._check(self.lib.wdm_adjoint(self.handle, int(nsteps), float(dt), int(ckpt_every), pt, wt,
+                                         None if d6 is None else C.c_void_p(d6.ctypes.data), pg, wg,
+                                         C.c_void_p(loss.ctypes.data), C.c_void_p(damp.ctypes.data)))
+        one = self.batch == 1
+        return (loss[0] if one else loss), grad_out, (None if d6 is None else (damp[0] if one else damp))
+
     def kick(self, dt, t=0.0):
         self._check(self.lib.wdm_kick(self.handle, float(dt), float(t)))
 

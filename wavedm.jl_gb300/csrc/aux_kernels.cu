@@ -13,6 +13,37 @@ __global__ void k_sincos_half(const float* __restrict__ h, float* __restrict__ o
   }
 }
 
+__global__ void k_adj_seed(const float2* __restrict__ psi, const float* __restrict__ rho_t, float2* __restrict__ lam,
+                           long long n, double dV, double* __restrict__ loss) {
+  const long long off = blockIdx.y * n;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = psi[off + i];
+    const float d = p.x * p.x + p.y * p.y - rho_t[off + i];
+    const float s = (float)(4.0 * dV) * d;
+    lam[off + i] = make_float2(s * p.x, s * p.y);
+    acc += (double)d * d;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
+    atomicAdd(loss + blockIdx.y, s * dV);
+  }
+}
+
+cudaError_t launch_adj_seed(const float2* psi, const float* rho_t, float2* lam, long long n, int batch, double dV,
+                            double* loss, cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 608) blocks = 608;
+  k_adj_seed<<<dim3((unsigned)blocks, batch), 256, 0, st>>>(psi, rho_t, lam, n, dV, loss);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sincos_half(const float* h, float* out, long long n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const long long b = (n + 255) / 256;

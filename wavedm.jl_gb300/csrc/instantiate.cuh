@@ -131,9 +131,33 @@ struct Launch {
     fill_stage_twiddles<N>(XF{}, out + TW_X_FWD * N, make);
     fill_stage_twiddles<N>(typename Reverse<XF>::type{}, out + TW_X_REV * N, make);
   }
+  static cudaError_t adj_kick(float2* lam, const float2* H, float2* Hmu, const RowGeom& rg, long long hpitch,
+                              long long hbstride, const float4* tw, const KickArgs& a, const AdjArgs& j, int batch,
+                              cudaStream_t st) {
+    cudaError_t e;
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
+    if ((e = prep_once<k_xw_adj_kick<N>>(XSMEM)) != cudaSuccess) return e;
+    k_xw_adj_kick<N><<<gr, XNT, XSMEM, st>>>(lam, H, Hmu, rg, hpitch, hbstride, tw, a, j, w);
+    return cudaGetLastError();
+  }
+  static cudaError_t adj_apply(float2* lam, const float2* Hmu, const RowGeom& rg, long long hpitch, long long hbstride,
+                               const float4* tw, const AdjArgs& j, bool fwd, int batch, cudaStream_t st) {
+    cudaError_t e;
+    XWork w;
+    const dim3 gr = grid_x(rg, batch, &w);
+    if (fwd) {
+      if ((e = prep_once<k_xw_adj_apply<N, true>>(XSMEM)) != cudaSuccess) return e;
+      k_xw_adj_apply<N, true><<<gr, XNT, XSMEM, st>>>(lam, Hmu, rg, hpitch, hbstride, tw, j, w);
+    } else {
+      if ((e = prep_once<k_xw_adj_apply<N, false>>(XSMEM)) != cudaSuccess) return e;
+      k_xw_adj_apply<N, false><<<gr, XNT, XSMEM, st>>>(lam, Hmu, rg, hpitch, hbstride, tw, j, w);
+    }
+    return cudaGetLastError();
+  }
   static const KernelSet* set() {
-    static const KernelSet ks = {N, &lfft, &lfft_drift, &lfft_poisson, &xfft, &x_inv_rho, &x_kick, &x_c2r, &x_r2c,
-                                 &fill_twiddles};
+    static const KernelSet ks = {N,          &lfft,  &lfft_drift,    &lfft_poisson, &xfft,     &x_inv_rho,
+                                 &x_kick,    &x_c2r, &x_r2c,         &fill_twiddles, &adj_kick, &adj_apply};
     return &ks;
   }
 };

@@ -3,7 +3,7 @@
 // build parallelises) and exposes wdm_ks_<N>().
 #pragma once
 #include <cuda_runtime.h>
-#include "passes.cuh"
+#include "xpass_warp.cuh"
 
 namespace wdm {
 
@@ -28,6 +28,12 @@ struct KernelSet {
                        const float4* tw, const float* shift, int batch, cudaStream_t st);
   // host: fill the TW_TABLES x n stage-major twiddle tables of this axis length
   void (*fill_twiddles)(float4* out);
+  // adjoint x passes (xpass_warp.cuh)
+  cudaError_t (*adj_kick)(float2* lam, const float2* H, float2* Hmu, const RowGeom& rg, long long hpitch,
+                          long long hbstride, const float4* tw, const KickArgs& a, const AdjArgs& j, int batch,
+                          cudaStream_t st);
+  cudaError_t (*adj_apply)(float2* lam, const float2* Hmu, const RowGeom& rg, long long hpitch, long long hbstride,
+                           const float4* tw, const AdjArgs& j, bool fwd, int batch, cudaStream_t st);
 };
 
 const KernelSet* kernels_for(int n);

@@ -90,6 +90,7 @@ struct DriftOp {
   const float* kz2;
   float half_dt;
   float scale;
+  float sign;             // +1: exp(-i k^2 dt/2); -1: its conjugate (the drift adjoint)
   int nxa;
   int precise;
   long long tab_bstride;  // per-batch-item stride of the phase tables (0 = shared)
@@ -105,11 +106,11 @@ struct DriftOp {
       const float lo = ((e1 + e2) + (tx.y + ty.y)) + tz.y;
       const float n = rintf(s2 * 0.15915494309189535f);
       const float r = fmaf(-n, 6.28318548202514648f, s2) + fmaf(-n, -1.7484555e-07f, lo);
-      const float2 em1 = expm1_neg_i(r);  // exp(-i r) - 1
+      const float2 em1 = expm1_neg_i(sign * r);  // exp(-i r) - 1 (or its conjugate)
       const float2 w = cadd(v, cmul(v, em1));
       return make_float2(fmaf(w.x, scale, w.x * scale_lo), fmaf(w.y, scale, w.y * scale_lo));
     }
-    const float th = (kx2[mx] + ky2[my] + kz2[pos]) * half_dt;
+    const float th = sign * (kx2[mx] + ky2[my] + kz2[pos]) * half_dt;
     float s, c;
     sincosf(th, &s, &c);
     return cmul(v, make_float2(c * scale, -s * scale));

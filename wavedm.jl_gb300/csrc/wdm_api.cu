@@ -124,6 +124,13 @@ struct wdm_ctx {
   int have_psi = 0;
   int phi_valid = 0;
   int64_t launch_count = 0;
+  // adjoint buffers (allocated on first use)
+  float2* lam = nullptr;            // adjoint state [batch][ncell]
+  float2* Hmu = nullptr;            // half spectrum of mu
+  float* rho_t = nullptr;           // target density
+  float* D6 = nullptr;              // tidal direction
+  double* adj_acc = nullptr;        // [2 batch]: loss, dL/da
+  std::vector<float2*> ck_psi, ck_H, slot_psi, slot_H;  // checkpoints / segment states
   long long version = 0;            // bumped by every set_* call that a captured graph bakes in
   struct wdm_group* self_group = nullptr;  // single-member group of wdm_step_graph
   Profiler prof;
@@ -448,10 +455,14 @@ static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd) {
   return WDM_OK;
 }
 
-// P2..P4 on x-spectral psi: y fwd, z fwd * drift phase * inverse, y inverse.
-static wdm_status drift_yz(wdm_ctx* c, double dt) {
+// P2..P4 on x-spectral data (psi, or `data` when given): y fwd, z fwd * drift
+// phase * inverse, y inverse.  sign = -1 applies the conjugate phase (the
+// drift adjoint).
+static wdm_status drift_yz(wdm_ctx* c, double dt, float sign = 1.f, float2* data = nullptr) {
   const int B = c->d.batch;
+  float2* psi = data ? data : c->psi;
   DriftOp op{};
+  op.sign = sign;
   const bool precise = c->d.phase_mode == WDM_PHASE_PRECISE;
   if (precise) WDM_TRY(ensure_drift_tables(c, dt));
   op.cx = c->cx;
@@ -469,15 +480,15 @@ static wdm_status drift_yz(wdm_ctx* c, double dt) {
   op.tab_bstride = 0;
   cudaError_t e;
   if ((e = run_pass(c, P_PSI_Y_FWD,
-                    [&] { return c->ky->lfft(c->psi, lines_y(c, c->d.nx, c->ncell), c->twy, false, B, c->st); })) !=
+                    [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->ncell), c->twy, false, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "psi y fwd");
   if ((e = run_pass(c, P_PSI_Z_DRIFT,
-                    [&] { return c->kz->lfft_drift(c->psi, lines_z(c, c->d.nx, c->ncell), c->twz, op, B, c->st); })) !=
+                    [&] { return c->kz->lfft_drift(psi, lines_z(c, c->d.nx, c->ncell), c->twz, op, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "psi z drift");
   if ((e = run_pass(c, P_PSI_Y_INV,
-                    [&] { return c->ky->lfft(c->psi, lines_y(c, c->d.nx, c->ncell), c->twy, true, B, c->st); })) !=
+                    [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->ncell), c->twy, true, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "psi y inv");
   return WDM_OK;
@@ -551,6 +562,12 @@ wdm_status wdm_destroy(wdm_ctx* c) {
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
     if (p) cudaFree(p);
+  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc};
+  for (void* p : adj)
+    if (p) cudaFree(p);
+  for (auto* v : {&c->ck_psi, &c->ck_H, &c->slot_psi, &c->slot_H})
+    for (float2* p : *v)
+      if (p) cudaFree(p);
   for (auto& r : c->prof.pending) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -1004,6 +1021,146 @@ wdm_status wdm_check_finite(wdm_ctx* c, int32_t* finite) {
   if (fault_injected("nonfinite")) flag = 1;
   *finite = flag ? 0 : 1;
   return WDM_OK;
+}
+
+// --------------------------------------------------------------------------
+// Adjoint of a Strang run (checkpointed)
+// --------------------------------------------------------------------------
+// A Strang run of N steps is N+1 kicks at the boundaries b = 0..N (dt/2, dt,
+// ..., dt, dt/2; consecutive half kicks see the same density and merge) and N
+// drifts.  s_b is the state just before the kick of boundary b; the forward
+// pass keeps (s_b, H_b) every ck steps, the reverse sweep recomputes the
+// states of one segment at a time and runs the adjoint kick (A1, Poisson of mu,
+// A5) and the adjoint drift (conjugate phase) boundary by boundary.
+static wdm_status ensure_pairs(wdm_ctx* c, std::vector<float2*>& ps, std::vector<float2*>& hs, size_t n) {
+  const size_t B = (size_t)c->d.batch;
+  while (ps.size() < n) {
+    float2 *p = nullptr, *h = nullptr;
+    WDM_TRY(dalloc(c, &p, B * c->ncell));
+    ps.push_back(p);
+    wdm_status s = dalloc(c, &h, B * c->nhalf);
+    if (s != WDM_OK) return s;
+    hs.push_back(h);
+  }
+  return WDM_OK;
+}
+
+static wdm_status copy_pair(wdm_ctx* c, float2* dp, float2* dh, const float2* sp, const float2* sh) {
+  const size_t B = (size_t)c->d.batch;
+  WDM_CU(c, cudaMemcpyAsync(dp, sp, sizeof(float2) * B * c->ncell, cudaMemcpyDeviceToDevice, c->st));
+  WDM_CU(c, cudaMemcpyAsync(dh, sh, sizeof(float2) * B * c->nhalf, cudaMemcpyDeviceToDevice, c->st));
+  return WDM_OK;
+}
+
+// one boundary of the forward run: kick of boundary b, drift, density and Poisson
+static wdm_status forward_boundary(wdm_ctx* c, int b, double dt) {
+  WDM_TRY(kick(c, b == 0 ? 0.5 * dt : dt, b, true));
+  WDM_TRY(drift_yz(c, dt));
+  return density_poisson(c, 1, dt);
+}
+
+static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const float* rho_target, int where_t,
+                               const double* tidal_dir, void* grad, int where_g, double* loss, double* damp) {
+  WDM_TRY(need_psi(c));
+  if (nsteps < 1 || ck < 1) return fail(c, WDM_ERR_INVALID, "wdm_adjoint: nsteps and ckpt_every must be >= 1");
+  if (!rho_target || !grad || !loss) return fail(c, WDM_ERR_INVALID, "wdm_adjoint: null argument");
+  if (c->tide_on == 1) {
+    const size_t have = c->tide.size() / 6;
+    if (have != 1 && have < (size_t)nsteps + 1)
+      return fail(c, WDM_ERR_INVALID, "wdm_adjoint: tidal schedule needs nsteps+1 rows (or exactly 1)");
+  }
+  const int B = c->d.batch;
+  const size_t nc = (size_t)B * c->ncell, nh = (size_t)B * c->nhalf;
+  if (!c->lam) WDM_TRY(dalloc(c, &c->lam, nc));
+  if (!c->Hmu) WDM_TRY(dalloc(c, &c->Hmu, nh));
+  if (!c->rho_t) WDM_TRY(dalloc(c, &c->rho_t, nc));
+  if (!c->D6) WDM_TRY(dalloc(c, &c->D6, 6));
+  if (!c->adj_acc) WDM_TRY(dalloc(c, &c->adj_acc, (size_t)2 * B));
+  const int nck = nsteps / ck + 1;
+  WDM_TRY(ensure_pairs(c, c->ck_psi, c->ck_H, (size_t)nck));
+  WDM_TRY(ensure_pairs(c, c->slot_psi, c->slot_H, (size_t)ck + 1));
+  WDM_TRY(copy_in(c, c->rho_t, rho_target, sizeof(float) * nc, where_t));
+  if (tidal_dir) {
+    float d6[6];
+    for (int q = 0; q < 6; ++q) d6[q] = (float)tidal_dir[q];
+    WDM_CU(c, cudaMemcpyAsync(c->D6, d6, sizeof(d6), cudaMemcpyHostToDevice, c->st));
+  }
+  WDM_CU(c, cudaMemsetAsync(c->adj_acc, 0, sizeof(double) * 2 * B, c->st));
+  if (c->d.phase_mode == WDM_PHASE_PRECISE) WDM_TRY(ensure_drift_tables(c, dt));
+  if (c->d.absorb_alpha != 0.0) WDM_TRY(ensure_mask_tables(c, dt));
+  if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
+  // forward: checkpoints of (s_b, H_b) at b = 0, ck, 2 ck, ...
+  WDM_TRY(copy_pair(c, c->ck_psi[0], c->ck_H[0], c->psi, c->H));
+  for (int b = 0; b < nsteps; ++b) {
+    WDM_TRY(forward_boundary(c, b, dt));
+    if ((b + 1) % ck == 0) WDM_TRY(copy_pair(c, c->ck_psi[(b + 1) / ck], c->ck_H[(b + 1) / ck], c->psi, c->H));
+  }
+  WDM_TRY(kick(c, 0.5 * dt, nsteps, false));  // psi_N
+  cudaError_t e = launch_adj_seed(c->psi, c->rho_t, c->lam, c->ncell, B, c->dx * c->dy * c->dz, c->adj_acc, c->st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "adjoint seed");
+  if ((e = c->kx->xfft(c->lam, rows_psi(c), c->twx, false, (float)(1.0 / c->d.nx), B, c->st)) != cudaSuccess)
+    return cuda_fail(c, e, "adjoint x fwd");
+  AdjArgs j{};
+  j.D6 = tidal_dir ? c->D6 : nullptr;
+  j.damp = c->adj_acc + B;
+  const bool mask = c->d.absorb_alpha != 0.0;
+  j.mx = mask ? c->mx : nullptr;
+  j.my = mask ? c->my : nullptr;
+  j.mz = mask ? c->mz : nullptr;
+  PoissonOp po;
+  po.kx2 = c->kx2;
+  po.ky2 = c->ky2;
+  po.kz2 = c->kz2;
+  po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
+  po.nxa = c->nxh;
+  for (int seg = (nsteps - 1) / ck; seg >= 0; --seg) {
+    const int j0 = seg * ck, j1 = std::min(j0 + ck, nsteps);
+    // recompute s_{j0..j1} of this segment into the slots
+    WDM_TRY(copy_pair(c, c->psi, c->H, c->ck_psi[seg], c->ck_H[seg]));
+    WDM_TRY(copy_pair(c, c->slot_psi[0], c->slot_H[0], c->psi, c->H));
+    for (int b = j0; b < j1; ++b) {
+      WDM_TRY(forward_boundary(c, b, dt));
+      WDM_TRY(copy_pair(c, c->slot_psi[b + 1 - j0], c->slot_H[b + 1 - j0], c->psi, c->H));
+    }
+    const int blo = (j0 == 0) ? 0 : j0 + 1;
+    for (int b = j1; b >= blo; --b) {
+      const double dtk = (b == 0 || b == nsteps) ? 0.5 * dt : dt;
+      KickArgs ka = kick_args(c, dtk, b);
+      j.pre = c->slot_psi[b - j0];
+      const float2* Hb = c->slot_H[b - j0];
+      if ((e = c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->nxh, c->nhalf, c->twx, ka, j, B, c->st)) !=
+          cudaSuccess)
+        return cuda_fail(c, e, "adjoint kick");
+      if ((e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess ||
+          (e = c->kz->lfft_poisson(c->Hmu, lines_z(c, c->nxh, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess ||
+          (e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
+        return cuda_fail(c, e, "adjoint Poisson");
+      if ((e = c->kx->adj_apply(c->lam, c->Hmu, rows_psi(c), c->nxh, c->nhalf, c->twx, j, b > 0, B, c->st)) !=
+          cudaSuccess)
+        return cuda_fail(c, e, "adjoint apply");
+      c->launch_count += 5;
+      if (b > 0) WDM_TRY(drift_yz(c, dt, -1.f, c->lam));
+    }
+  }
+  // leave the context at psi_0 with its potential
+  WDM_TRY(copy_pair(c, c->psi, c->H, c->ck_psi[0], c->ck_H[0]));
+  c->phi_valid = 1;
+  WDM_TRY(copy_out(c, grad, c->lam, sizeof(float2) * nc, where_g));
+  std::vector<double> acc((size_t)2 * B);
+  WDM_CU(c, cudaMemcpy(acc.data(), c->adj_acc, sizeof(double) * 2 * B, cudaMemcpyDeviceToHost));
+  for (int b = 0; b < B; ++b) {
+    loss[b] = acc[b];
+    if (damp) damp[b] = acc[B + b];
+  }
+  return sync_and_check(c);
+}
+
+extern "C" wdm_status wdm_adjoint(wdm_ctx* c, int32_t nsteps, double dt, int32_t ckpt_every, const float* rho_target,
+                                  int32_t where_target, const double* tidal_dir, void* grad, int32_t where_grad,
+                                  double* loss, double* dloss_damp) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  return adjoint_impl(c, nsteps, dt, ckpt_every, rho_target, where_target, tidal_dir, grad, where_grad, loss,
+                      dloss_damp);
 }
 
 // --------------------------------------------------------------------------

@@ -473,6 +473,170 @@ k_xw_r2c(const float* __restrict__ in, float2* __restrict__ H, RowGeom rg, long 
   }
 }
 
+// ----------------------------------------------------------------------------
+// Adjoint passes.  For a kick psi+ = exp(-i th) psi (th = dt_k (Phi + V + tide +
+// kappa |psi|^2)) the adjoint of lam+ is
+//   lam = exp(i th) lam+ + 2 (G mu + kappa mu) psi,  mu = dt_k Im(conj(lam+) psi+),
+// with G the Poisson operator; a tidal amplitude a (tide = a D) adds
+// dL/da += sum mu (1/2 x^T D x).  A1 does the x-inverse of lam, the pointwise
+// part and the packed R2C of mu; A5 adds 2 G(mu) psi after the Poisson solve,
+// the absorbing mask and (FWD) the x-forward transform of the drift adjoint.
+// ----------------------------------------------------------------------------
+struct AdjArgs {
+  const float2* pre;      // pre-kick state psi [batch][nz][ny][nx] (real space)
+  const float* D6;        // tidal direction (xx, yy, zz, xy, xz, yz) or null
+  double* damp;           // [batch] accumulators of dL/da
+  const float* mx;        // absorbing-mask tables (A5, null: none)
+  const float* my;
+  const float* mz;
+};
+
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
+k_xw_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __restrict__ Hmu, RowGeom rg,
+              long long hpitch, long long hbstride, const float4* __restrict__ twg, KickArgs a, AdjArgs j, XWork w) {
+  WDM_XPASS_PROLOGUE
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+    const float2* hrow = H + b * hbstride + ra * hpitch;
+    float2 v[N / T];
+    // potential rows of the pair, at the radix-RS slots
+    load_packed_half<N, T, R1>(v, hrow, hrow + hpitch, ok, t);
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
+    float phi[2][N / T];
+#pragma unroll
+    for (int q = 0; q < N / T; ++q) {
+      phi[0][q] = v[q].x;
+      phi[1][q] = v[q].y;
+    }
+    float T6[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
+    float mu0[N / T];
+    float2 z[N / T];
+    float damp = 0.f;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int r = ra + half;
+      float2* row = lam + b * rg.bstride + (long long)r * rg.pitch;
+      const float2* prow = j.pre + b * rg.bstride + (long long)r * rg.pitch;
+      const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+      run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // lam+ in real space, radix-RS slots
+      const int y = r % rg.ny, zc = r / rg.ny;
+      const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * zc;
+      const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
+      const float lin = T6[3] * fy + T6[4] * fz;
+      float dyz = 0.f, dlin = 0.f;
+      if (j.D6) {
+        dyz = 0.5f * j.D6[1] * fy * fy + j.D6[5] * fy * fz + 0.5f * j.D6[2] * fz * fz;
+        dlin = j.D6[3] * fy + j.D6[4] * fz;
+      }
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) {
+          const int q = i * RS + k;
+          const int x = slot_pos<N, T, RS>(t, i, k);
+          const float2 pre = ok ? prow[x] : make_float2(0.f, 0.f);
+          const float fx = a.x0 + a.dx * x;
+          float pot = phi[half][q];
+          if (a.tidal) pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
+          if (a.kerr != 0.f) pot += a.kerr * (pre.x * pre.x + pre.y * pre.y);
+          if (vrow && ok) pot += vrow[x];
+          const float2 post = apply_kick(pre, pot, a);
+          const float2 lp = v[q];
+          const float mu = a.dt_hi * (lp.x * post.y - lp.y * post.x);
+          float2 ln = apply_kick(lp, -pot, a);  // exp(+i th) lam+
+          if (a.kerr != 0.f) {
+            ln.x = fmaf(2.f * a.kerr * mu, pre.x, ln.x);
+            ln.y = fmaf(2.f * a.kerr * mu, pre.y, ln.y);
+          }
+          if (j.D6) damp = fmaf(mu, fmaf(fx, fmaf(0.5f * j.D6[0], fx, dlin), dyz), damp);
+          if (ok) row[x] = ln;
+          if (half == 0) mu0[q] = mu;
+          else z[q] = make_float2(mu0[q], mu);
+        }
+    }
+    reorder<N, T, RS, R1>(z, v);
+    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+    float2* hm = Hmu + b * hbstride + ra * hpitch;
+    store_packed_half<N, T, RS>(v, buf, hm, hm + hpitch, ok, t);
+    if (j.D6) {
+      // sum over the T lanes of this group only (groups of one warp may hold
+      // rows of different batch items)
+#pragma unroll
+      for (int off = T / 2; off > 0; off >>= 1) damp += __shfl_down_sync(0xffffffffu, damp, off, T);
+      if (t == 0 && ok) atomicAdd(j.damp + b, (double)damp);
+    }
+  }
+}
+
+template <int N, bool FWD>
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
+k_xw_adj_apply(float2* __restrict__ lam, const float2* __restrict__ Hmu, RowGeom rg, long long hpitch,
+               long long hbstride, const float4* __restrict__ twg, AdjArgs j, XWork w) {
+  WDM_XPASS_PROLOGUE
+  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+    const long long pp = u * C::GROUPS + g;
+    const bool ok = pp < (long long)w.pairs_per_item * w.batch;
+    const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
+    const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
+    const float2* hrow = Hmu + b * hbstride + ra * hpitch;
+    float2 v[N / T];
+    load_packed_half<N, T, R1>(v, hrow, hrow + hpitch, ok, t);
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // G mu of rows A, B at radix-RS slots
+    float gmu[2][N / T];
+#pragma unroll
+    for (int q = 0; q < N / T; ++q) {
+      gmu[0][q] = v[q].x;
+      gmu[1][q] = v[q].y;
+    }
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int r = ra + half;
+      float2* row = lam + b * rg.bstride + (long long)r * rg.pitch;
+      const float2* prow = j.pre + b * rg.bstride + (long long)r * rg.pitch;
+      const float myz = j.mx ? j.my[r % rg.ny] * j.mz[r / rg.ny] : 1.f;
+      float2 zz[N / T];
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) {
+          const int q = i * RS + k;
+          const int x = slot_pos<N, T, RS>(t, i, k);
+          float2 l = ok ? row[x] : make_float2(0.f, 0.f);
+          const float2 pre = ok ? prow[x] : make_float2(0.f, 0.f);
+          l.x = fmaf(2.f * gmu[half][q], pre.x, l.x);
+          l.y = fmaf(2.f * gmu[half][q], pre.y, l.y);
+          if (FWD && j.mx) l = cscale(l, myz * j.mx[x]);  // the mask precedes every kick but the first
+          zz[q] = l;
+        }
+      if constexpr (FWD) {
+        reorder<N, T, RS, R1>(zz, v);
+        run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+        if (ok)
+#pragma unroll
+          for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+            for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+      } else {
+        if (ok)
+#pragma unroll
+          for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+            for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = zz[i * RS + k];
+      }
+    }
+  }
+}
+
 #undef WDM_XPASS_PROLOGUE
 
 }  // namespace wdm
