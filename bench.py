@@ -376,6 +376,59 @@ def time_oracle(wl, budget_s, max_steps, warm=1):
     return n / el, n, spe.WORKERS
 
 
+def run_adjoint(args, rank, world):
+    """Workload 5: adjoint of 200 Strang steps at 128^3 (checkpoints every 20) vs the forward run."""
+    import torch
+
+    import wavedm_gb300 as wdm
+
+    wdm.build_library()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    ics = wdm.ics
+    N, L = args.n or 128, 20.0
+    nsteps, ck = 200, 20
+    dt = ics.dt_for(N, L)
+    D = np.array([2.0, -1.0, -1.0, 0.0, 0.0, 0.0])
+    amp, rc = 0.02, 1.2
+    psi0 = ics.soliton_halo_ic((N, N, N), (L, L, L), rc=rc, rng=ics.rng_for(5)).astype(np.complex64)
+    target = (np.abs(ics.soliton_halo_ic((N, N, N), (L, L, L), rc=1.1 * rc, rng=ics.rng_for(5))) ** 2
+              ).astype(np.float32)
+    ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=1.0, phase_mode=args.phase)
+    ctx.set_psi(psi0)
+    ctx.set_tidal([amp * D])
+    rho_d = torch.from_numpy(target).cuda()
+    grad_d = torch.empty(psi0.shape, dtype=torch.complex64, device="cuda")
+    # warm-up of both
+    ctx.step(nsteps, dt)
+    ctx.set_psi(psi0)
+    ctx.adjoint(nsteps, dt, rho_d, ckpt_every=ck, tidal_dir=D, grad_out=grad_d)
+    torch.cuda.synchronize()
+    reps = max(1, args.steps // 10)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.set_psi(psi0)
+        ctx.step(nsteps, dt)
+    t_fwd = (time.perf_counter() - t0) / reps
+    l0 = ctx.launch_count
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.set_psi(psi0)
+        loss, _, da = ctx.adjoint(nsteps, dt, rho_d, ckpt_every=ck, tidal_dir=D, grad_out=grad_d)
+    t_adj = (time.perf_counter() - t0) / reps
+    launches = (ctx.launch_count - l0) // reps
+    ctx.close()
+    return {
+        "metric": f"adjoint/forward time ratio, {nsteps} Strang steps at {N}^3, checkpoints every {ck}",
+        "value": round(t_adj / t_fwd, 3), "unit": "ratio", "n_gpus": world, "steps": nsteps, "warmup": nsteps,
+        "ms_per_step": round(t_adj / nsteps * 1e3, 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded soliton + halo; target from rc x 1.1)",
+        "config": {"workload": "adjoint128", "grid": [N, N, N], "dt": dt, "ckpt_every": ck, "repeats": reps,
+                   "phase_mode": args.phase},
+        "forward_steps_per_s": round(nsteps / t_fwd, 2), "adjoint_steps_per_s": round(nsteps / t_adj, 2),
+        "loss": float(loss), "dL_damp": float(da), "gpu_launches": int(launches),
+    }
+
+
 def ensemble_cpu_baseline(budget_s):
     """Oracle time of one step of one halo per size, weighted by the halo counts."""
     import wavedm_gb300 as wdm
@@ -450,6 +503,15 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.workload == 5:
+        rec = run_adjoint(args, rank, world)
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+        if rank == 0:
+            print(json.dumps(rec), flush=True)
+        return
     if args.workload == 4:
         rec = run_ensemble(args, rank, world)
         if rank == 0 and not args.no_cpu_baseline:

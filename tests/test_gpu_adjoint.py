@@ -43,6 +43,26 @@ def test_adjoint_matches_fp64_adjoint(wdm, kerr, alpha, ckpt):
     assert np.array_equal(psi_after, psi0)
 
 
+def test_autograd_function_matches_fp64_adjoint(wdm):
+    torch = pytest.importorskip("torch")
+    from wavedm_gb300.autograd import evolve_loss
+
+    g, psi0, D, amp, target = _case(n=32)
+    dt, nsteps = 0.03, 8
+    phys = spe.Physics(poisson_coeff=1.5, tidal=lambda t: tuple(amp * D))
+    L_ref, g_ref, da_ref = adj.adjoint(psi0.astype(np.complex128), g, phys, dt, nsteps,
+                                       target.astype(np.float64), tidal_dir=D)
+    p = torch.from_numpy(psi0).cuda().requires_grad_(True)
+    a = torch.tensor(amp, dtype=torch.float64, requires_grad=True)
+    rho = torch.from_numpy(target).cuda()
+    with wdm.SPEContext(g.n, g.L, poisson_coeff=1.5) as ctx:
+        loss = evolve_loss(p, a, ctx, nsteps, dt, rho, D, ckpt_every=3)
+        (2.0 * loss).backward()
+    assert float(loss) == pytest.approx(L_ref, rel=1e-5)
+    assert spe.rel_l2(p.grad.cpu().numpy() / 2.0, g_ref) < 5e-4
+    assert float(a.grad) / 2.0 == pytest.approx(da_ref, rel=1e-3)
+
+
 def test_adjoint_workload5_shape_at_64(wdm):
     """The adjoint workload's loss and parameters on a 64^3 grid, against the FP64
     CPU adjoint, including dL/drc through the chain rule of the initial state
