@@ -235,15 +235,18 @@ namespace wdm {
 // the launcher), then shift[b] = sums[b] / n + add.
 template <bool COMPLEX>
 __global__ void k_block_sum(const void* __restrict__ data, long long n, double* __restrict__ sums) {
-  double acc = 0.0;
+  // per-thread FP32 partial sums (the shift only needs to be near the mean:
+  // any value is exact), FP64 from the warp reduction on
+  float accf = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     if constexpr (COMPLEX) {
       const float2 v = static_cast<const float2*>(data)[blockIdx.y * n + i];
-      acc += (double)v.x * v.x + (double)v.y * v.y;
+      accf = fmaf(v.x, v.x, fmaf(v.y, v.y, accf));
     } else {
-      acc += (double)static_cast<const float*>(data)[blockIdx.y * n + i];
+      accf += static_cast<const float*>(data)[blockIdx.y * n + i];
     }
   }
+  double acc = accf;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
   __shared__ double sh[32];

@@ -14,39 +14,66 @@ static cudaError_t prep_once(size_t smem) {
   return e;
 }
 
+// SMs of the current device (queried once).
+static int sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+// Resident CTAs per SM of a kernel at its block size and shared memory (once).
+template <auto K>
+static int resident_ctas(int threads, size_t smem) {
+  static const int n = [&] {
+    int v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, K, threads, smem);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
 template <int N>
 struct Launch {
   static constexpr int NT = threads_for<N>();
-  static constexpr size_t SM = smem_bytes<N>();
-  static constexpr size_t SMID = smem_bytes_mid<N>();
 
-  static dim3 grid_lines(int nlines, int batch) { return dim3((nlines + LINES - 1) / LINES, batch); }
+  // persistent line pass: one wave of resident CTAs walking all tiles
+  template <int MODE, class Op>
+  static cudaError_t lpipe(float2* data, const LineGeom& g, const float4* tw, const Op& op, int batch,
+                           cudaStream_t st) {
+    if (g.nlines <= 0 || batch <= 0) return cudaSuccess;
+#ifndef WDM_LINE_PIPELINE
+    {
+      constexpr size_t SMEM = ltile_smem_bytes<N, MODE>();
+      cudaError_t e;
+      if ((e = prep_once<k_lfft_tile<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
+      k_lfft_tile<N, MODE, Op><<<dim3((g.nlines + LINES - 1) / LINES, batch), NT, SMEM, st>>>(data, g, tw, op);
+      return cudaGetLastError();
+    }
+#endif
+    constexpr size_t SMEM = lpipe_smem_bytes<N, MODE>();
+    cudaError_t e;
+    if ((e = prep_once<k_lfft_pipe<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
+    const long long tiles = (long long)((g.nlines + LINES - 1) / LINES) * batch;
+    const long long cap = (long long)resident_ctas<k_lfft_pipe<N, MODE, Op>>(NT, SMEM) * sm_count();
+    const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
+    k_lfft_pipe<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, g, tw, op, batch);
+    return cudaGetLastError();
+  }
 
   static cudaError_t lfft(float2* data, const LineGeom& g, const float4* tw, bool inv, int batch, cudaStream_t st) {
-    if (g.nlines <= 0) return cudaSuccess;
-    cudaError_t e;
-    if (inv) {
-      if ((e = prep_once<k_lfft<N, true>>(SM)) != cudaSuccess) return e;
-      k_lfft<N, true><<<grid_lines(g.nlines, batch), NT, SM, st>>>(data, g, tw);
-    } else {
-      if ((e = prep_once<k_lfft<N, false>>(SM)) != cudaSuccess) return e;
-      k_lfft<N, false><<<grid_lines(g.nlines, batch), NT, SM, st>>>(data, g, tw);
-    }
-    return cudaGetLastError();
+    return inv ? lpipe<1>(data, g, tw, NoOp{}, batch, st) : lpipe<0>(data, g, tw, NoOp{}, batch, st);
   }
   static cudaError_t lfft_drift(float2* data, const LineGeom& g, const float4* tw, const DriftOp& op, int batch,
                                 cudaStream_t st) {
-    cudaError_t e;
-    if ((e = prep_once<k_lfft_mid<N, DriftOp>>(SMID)) != cudaSuccess) return e;
-    k_lfft_mid<N, DriftOp><<<grid_lines(g.nlines, batch), NT, SMID, st>>>(data, g, tw, op);
-    return cudaGetLastError();
+    return lpipe<2>(data, g, tw, op, batch, st);
   }
   static cudaError_t lfft_poisson(float2* data, const LineGeom& g, const float4* tw, const PoissonOp& op, int batch,
                                   cudaStream_t st) {
-    cudaError_t e;
-    if ((e = prep_once<k_lfft_mid<N, PoissonOp>>(SMID)) != cudaSuccess) return e;
-    k_lfft_mid<N, PoissonOp><<<grid_lines(g.nlines, batch), NT, SMID, st>>>(data, g, tw, op);
-    return cudaGetLastError();
+    return lpipe<2>(data, g, tw, op, batch, st);
   }
   // x passes: lane group per row pair, grid-stride over warp units
   static constexpr int XNT = XCfg<N>::NT;
@@ -83,17 +110,18 @@ struct Launch {
     k_xw_inv_rho<N><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
     return cudaGetLastError();
   }
-  static cudaError_t x_kick(float2* psi, const float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                            const float4* tw, const KickArgs& a, bool fwd, int batch, cudaStream_t st) {
+  static cudaError_t x_kick(const float2* psi_in, float2* psi, const float2* H, const RowGeom& rg, long long hpitch,
+                            long long hbstride, const float4* tw, const KickArgs& a, bool fwd, int batch,
+                            cudaStream_t st) {
     cudaError_t e;
     XWork w;
     const dim3 gr = grid_x(rg, batch, &w);
     if (fwd) {
       if ((e = prep_once<k_xw_kick<N, true>>(XSMEM)) != cudaSuccess) return e;
-      k_xw_kick<N, true><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
+      k_xw_kick<N, true><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
     } else {
       if ((e = prep_once<k_xw_kick<N, false>>(XSMEM)) != cudaSuccess) return e;
-      k_xw_kick<N, false><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
+      k_xw_kick<N, false><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
     }
     return cudaGetLastError();
   }

@@ -20,7 +20,8 @@ struct KernelSet {
                       cudaStream_t st);
   cudaError_t (*x_inv_rho)(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
                            const float4* tw, const RhoArgs& a, int batch, cudaStream_t st);
-  cudaError_t (*x_kick)(float2* psi, const float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
+  cudaError_t (*x_kick)(const float2* psi_in, float2* psi, const float2* H, const RowGeom& rg, long long hpitch,
+                        long long hbstride,
                         const float4* tw, const KickArgs& a, bool fwd, int batch, cudaStream_t st);
   cudaError_t (*x_c2r)(const float2* H, float* out, const RowGeom& rg, long long hpitch, long long hbstride,
                        const float4* tw, int batch, cudaStream_t st);

@@ -155,39 +155,114 @@ __device__ __forceinline__ void lines_store(const float2* v, float2* base, long 
     for (int k = 0; k < R; ++k) base[(long long)slot_pos<N, T, R>(t, i, k) * ps] = v[i * R + k];
 }
 
-template <int N, bool INV>
+// Persistent, double-buffered line pass.  Each CTA walks tiles of LINES lines
+// (grid-stride over all batch items).  While tile i is transformed in
+// registers (its exchanges reuse the buffer it arrived in), the cp.async copy
+// of tile i+1 into the other buffer is in flight, so the loads of a CTA never
+// wait behind its own arithmetic.  Thread (t, l) copies exactly the points
+// t + T m of line l that its first stage reads; 16 lanes of a half-warp copy
+// 16 neighbouring lines at one point, i.e. 128 contiguous bytes when the lines
+// are contiguous along x.
+// MODE: 0 forward, 1 inverse, 2 forward / op / inverse (fused k-space step).
+constexpr int LBUF = LINES;  // pitch of a tile buffer: point-major, one slot per line
+
+template <int N, int MODE>
+__host__ __device__ constexpr size_t lpipe_smem_bytes() {
+  return sizeof(float4) * (MODE == 2 ? 2 : 1) * N + 2 * sizeof(float2) * (size_t)N * LBUF;
+}
+
+template <int N>
+__device__ __forceinline__ void lines_issue(float2* buf, const LineGeom& g, float2* data, long long tile,
+                                            int tiles_per_item, int t, int l) {
+  constexpr int T = Plan<N>::T;
+  const int b = (int)(tile / tiles_per_item);
+  const int line = (int)(tile - (long long)b * tiles_per_item) * LINES + l;
+  if (line >= g.nlines) return;
+  const float2* base = data + b * g.bstride + line_base(g, line);
+#pragma unroll
+  for (int m = 0; m < N / T; ++m) {
+    const int p = t + T * m;
+    cp_async8(buf + p * LBUF + l, base + (long long)p * g.pstride);
+  }
+}
+
+template <int N, int MODE, class Op>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks<N>())
-k_lfft(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg) {
+k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op, int batch) {
   using P = Plan<N>;
   constexpr int T = P::T;
   using Rad = typename P::Fwd;
+  using Rev = typename Reverse<Rad>::type;
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
   extern __shared__ float2 smem[];
-  float4* tw = reinterpret_cast<float4*>(smem);
-  float2* s = smem + 2 * N;
-  load_twiddles(tw, twg + TW_LINE_FWD * N, N);
+  float4* tw = reinterpret_cast<float4*>(smem);  // line fwd [| line rev] tables
+  constexpr int NTAB = MODE == 2 ? 2 : 1;
+  float2* bufs = smem + 2 * NTAB * N;
+  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
   const int l = threadIdx.x % LINES, t = threadIdx.x / LINES;
-  const int line = blockIdx.x * LINES + l;
-  const bool ok = line < g.nlines;
-  float2* base = data + blockIdx.y * g.bstride + (ok ? line_base(g, line) : 0);
-  float2 v[N / T];
-  lines_load<N>(v, base, g.pstride, ok, t);
-  __syncthreads();
-  run_stages<N, T, LPITCH, INV>(Rad{}, v, s, tw, t, l);
-  lines_store<N, RadInfo<Rad>::last>(v, base, g.pstride, ok, t);
+  const int tiles_per_item = (g.nlines + LINES - 1) / LINES;
+  const long long total = (long long)tiles_per_item * batch;
+  long long tile = blockIdx.x;
+  if (tile < total) lines_issue<N>(bufs, g, data, tile, tiles_per_item, t, l);
+  cp_async_commit();
+  int cur = 0;
+  for (; tile < total; tile += gridDim.x) {
+    const long long nxt = tile + gridDim.x;
+    if (nxt < total) lines_issue<N>(bufs + (cur ^ 1) * N * LBUF, g, data, nxt, tiles_per_item, t, l);
+    cp_async_commit();
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    __syncthreads();
+    float2* s = bufs + cur * N * LBUF;
+    const int b = (int)(tile / tiles_per_item);
+    const int line = (int)(tile - (long long)b * tiles_per_item) * LINES + l;
+    const bool ok = line < g.nlines;
+    float2 v[N / T];
+    stage_read<N, T, R1, LBUF>(s, v, t, l);
+    if constexpr (MODE == 1) {
+      run_stages<N, T, LBUF, true>(Rad{}, v, s, tw, t, l);
+    } else {
+      run_stages<N, T, LBUF, false>(Rad{}, v, s, tw, t, l);
+    }
+    float2* base = data + b * g.bstride + (ok ? line_base(g, line) : 0);
+    if constexpr (MODE == 2) {
+      const int lc = ok ? line : 0;
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], lc, slot_pos<N, T, RS>(t, i, k), b);
+      run_stages<N, T, LBUF, true>(Rev{}, v, s, tw + N, t, l);
+      lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
+    } else {
+      lines_store<N, RS>(v, base, g.pstride, ok, t);
+    }
+    __syncthreads();  // the exchanges in s are done before s receives tile + 2 gridDim
+    cur ^= 1;
+  }
+  cp_async_wait_all();
 }
 
-template <int N, class Op>
+struct NoOp {
+  __device__ __forceinline__ float2 operator()(float2 v, int, int, int) const { return v; }
+};
+
+// One tile of LINES lines per CTA, loaded straight into registers (every
+// point of the tile in flight at once) and stored straight from them; the
+// hardware overlaps one resident CTA's loads with another's arithmetic.  This
+// is the default line pass (faster here than the persistent cp.async pipeline
+// above, which is kept behind WDM_LINE_PIPELINE for tuning).
+template <int N, int MODE, class Op>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks<N>())
-k_lfft_mid(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op) {
+k_lfft_tile(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op) {
   using P = Plan<N>;
   constexpr int T = P::T;
   using Rad = typename P::Fwd;
   using Rev = typename Reverse<Rad>::type;
   constexpr int RS = RadInfo<Rad>::last;
+  constexpr int NTAB = MODE == 2 ? 2 : 1;
   extern __shared__ float2 smem[];
-  float4* tw = reinterpret_cast<float4*>(smem);  // [line fwd | line rev] tables
-  float2* s = smem + 4 * N;
-  load_twiddles(tw, twg + TW_LINE_FWD * N, 2 * N);
+  float4* tw = reinterpret_cast<float4*>(smem);  // line fwd [| line rev] tables
+  float2* s = smem + 2 * NTAB * N;
+  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
   const int l = threadIdx.x % LINES, t = threadIdx.x / LINES;
   const int line = blockIdx.x * LINES + l;
   const bool ok = line < g.nlines;
@@ -195,15 +270,27 @@ k_lfft_mid(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg
   float2 v[N / T];
   lines_load<N>(v, base, g.pstride, ok, t);
   __syncthreads();
-  run_stages<N, T, LPITCH, false>(Rad{}, v, s, tw, t, l);
-  const int lc = ok ? line : 0;
+  if constexpr (MODE == 1) {
+    run_stages<N, T, LPITCH, true>(Rad{}, v, s, tw, t, l);
+  } else {
+    run_stages<N, T, LPITCH, false>(Rad{}, v, s, tw, t, l);
+  }
+  if constexpr (MODE == 2) {
+    const int lc = ok ? line : 0;
 #pragma unroll
-  for (int i = 0; i < N / (RS * T); ++i)
+    for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-    for (int k = 0; k < RS; ++k)
-      v[i * RS + k] = op(v[i * RS + k], lc, slot_pos<N, T, RS>(t, i, k), blockIdx.y);
-  run_stages<N, T, LPITCH, true>(Rev{}, v, s, tw + N, t, l);
-  lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
+      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], lc, slot_pos<N, T, RS>(t, i, k), blockIdx.y);
+    run_stages<N, T, LPITCH, true>(Rev{}, v, s, tw + N, t, l);
+    lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
+  } else {
+    lines_store<N, RS>(v, base, g.pstride, ok, t);
+  }
+}
+
+template <int N, int MODE>
+__host__ __device__ constexpr size_t ltile_smem_bytes() {
+  return sizeof(float2) * (size_t)(2 * (MODE == 2 ? 2 : 1) * N + N * LPITCH);
 }
 
 // ----------------------------------------------------------------------------

@@ -446,10 +446,12 @@ static KickArgs kick_args(const wdm_ctx* c, double dt, int sched_row) {
   return a;
 }
 
-static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd) {
+// Kick of psi (in place), or of psi_in into c->psi when psi_in is given.
+static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd, const float2* psi_in = nullptr) {
   KickArgs a = kick_args(c, dt, sched_row);
+  const float2* in = psi_in ? psi_in : c->psi;
   cudaError_t e = run_pass(c, fwd ? P_KICK_FWD : P_KICK, [&] {
-    return c->kx->x_kick(c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
+    return c->kx->x_kick(in, c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_kick");
   return WDM_OK;
@@ -1059,6 +1061,23 @@ static wdm_status forward_boundary(wdm_ctx* c, int b, double dt) {
   return density_poisson(c, 1, dt);
 }
 
+// The same boundary out of place: (psi_in, H_in) = s_b -> (psi_out, H_out) = s_{b+1}.
+// Keeps every state of a segment without copies.
+static wdm_status forward_boundary_to(wdm_ctx* c, int b, double dt, const float2* psi_in, float2* H_in,
+                                      float2* psi_out, float2* H_out) {
+  float2* keep_psi = c->psi;
+  float2* keep_H = c->H;
+  c->psi = psi_out;
+  c->H = H_in;
+  wdm_status s = kick(c, b == 0 ? 0.5 * dt : dt, b, true, psi_in);
+  if (s == WDM_OK) s = drift_yz(c, dt);
+  c->H = H_out;
+  if (s == WDM_OK) s = density_poisson(c, 1, dt);
+  c->psi = keep_psi;
+  c->H = keep_H;
+  return s;
+}
+
 static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const float* rho_target, int where_t,
                                const double* tidal_dir, void* grad, int where_g, double* loss, double* damp) {
   WDM_TRY(need_psi(c));
@@ -1089,13 +1108,27 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   if (c->d.phase_mode == WDM_PHASE_PRECISE) WDM_TRY(ensure_drift_tables(c, dt));
   if (c->d.absorb_alpha != 0.0) WDM_TRY(ensure_mask_tables(c, dt));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
-  // forward: checkpoints of (s_b, H_b) at b = 0, ck, 2 ck, ...
+  // forward: checkpoints of (s_b, H_b) at b = 0, ck, 2 ck, ...; the states of
+  // the last segment go straight into the slots (no recompute needed for it)
+  const int last_seg = (nsteps - 1) / ck, jl0 = last_seg * ck;
+  // state s_b of the segment starting at j0: the checkpoint or a slot
+  auto st_psi = [&](int seg, int b) { return b == seg * ck ? c->ck_psi[seg] : c->slot_psi[b - seg * ck]; };
+  auto st_H = [&](int seg, int b) { return b == seg * ck ? c->ck_H[seg] : c->slot_H[b - seg * ck]; };
   WDM_TRY(copy_pair(c, c->ck_psi[0], c->ck_H[0], c->psi, c->H));
-  for (int b = 0; b < nsteps; ++b) {
+  for (int b = 0; b < jl0; ++b) {
     WDM_TRY(forward_boundary(c, b, dt));
     if ((b + 1) % ck == 0) WDM_TRY(copy_pair(c, c->ck_psi[(b + 1) / ck], c->ck_H[(b + 1) / ck], c->psi, c->H));
   }
-  WDM_TRY(kick(c, 0.5 * dt, nsteps, false));  // psi_N
+  for (int b = jl0; b < nsteps; ++b)
+    WDM_TRY(forward_boundary_to(c, b, dt, st_psi(last_seg, b), st_H(last_seg, b), st_psi(last_seg, b + 1),
+                                st_H(last_seg, b + 1)));
+  {  // psi_N = final half kick of s_N, into the context's psi (psi_0 is kept in ck[0])
+    float2* keep_H = c->H;
+    c->H = st_H(last_seg, nsteps);
+    wdm_status s = kick(c, 0.5 * dt, nsteps, false, st_psi(last_seg, nsteps));
+    c->H = keep_H;
+    WDM_TRY(s);
+  }
   cudaError_t e = launch_adj_seed(c->psi, c->rho_t, c->lam, c->ncell, B, c->dx * c->dy * c->dz, c->adj_acc, c->st);
   if (e != cudaSuccess) return cuda_fail(c, e, "adjoint seed");
   if ((e = c->kx->xfft(c->lam, rows_psi(c), c->twx, false, (float)(1.0 / c->d.nx), B, c->st)) != cudaSuccess)
@@ -1113,21 +1146,18 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   po.kz2 = c->kz2;
   po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
   po.nxa = c->nxh;
-  for (int seg = (nsteps - 1) / ck; seg >= 0; --seg) {
+  for (int seg = last_seg; seg >= 0; --seg) {
     const int j0 = seg * ck, j1 = std::min(j0 + ck, nsteps);
-    // recompute s_{j0..j1} of this segment into the slots
-    WDM_TRY(copy_pair(c, c->psi, c->H, c->ck_psi[seg], c->ck_H[seg]));
-    WDM_TRY(copy_pair(c, c->slot_psi[0], c->slot_H[0], c->psi, c->H));
-    for (int b = j0; b < j1; ++b) {
-      WDM_TRY(forward_boundary(c, b, dt));
-      WDM_TRY(copy_pair(c, c->slot_psi[b + 1 - j0], c->slot_H[b + 1 - j0], c->psi, c->H));
-    }
+    // recompute s_{j0+1..j1} of this segment into the slots, out of place
+    if (seg != last_seg)
+      for (int b = j0; b < j1; ++b)
+        WDM_TRY(forward_boundary_to(c, b, dt, st_psi(seg, b), st_H(seg, b), st_psi(seg, b + 1), st_H(seg, b + 1)));
     const int blo = (j0 == 0) ? 0 : j0 + 1;
     for (int b = j1; b >= blo; --b) {
       const double dtk = (b == 0 || b == nsteps) ? 0.5 * dt : dt;
       KickArgs ka = kick_args(c, dtk, b);
-      j.pre = c->slot_psi[b - j0];
-      const float2* Hb = c->slot_H[b - j0];
+      j.pre = st_psi(seg, b);
+      const float2* Hb = st_H(seg, b);
       if ((e = c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->nxh, c->nhalf, c->twx, ka, j, B, c->st)) !=
           cudaSuccess)
         return cuda_fail(c, e, "adjoint kick");

@@ -252,8 +252,9 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
 // ----------------------------------------------------------------------------
 template <int N, bool FWD>
 __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
-k_xw_kick(float2* __restrict__ psi, const float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
-          const float4* __restrict__ twg, KickArgs a, XWork w) {
+k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGeom rg, long long hpitch,
+          long long hbstride, const float4* __restrict__ twg, KickArgs a, XWork w) {
+  // psi_in == psi runs in place; a separate psi_in keeps the input state
   WDM_XPASS_PROLOGUE
   using Rev = typename Reverse<Rad>::type;
   for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
@@ -278,11 +279,12 @@ k_xw_kick(float2* __restrict__ psi, const float2* __restrict__ H, RowGeom rg, lo
     for (int half = 0; half < 2; ++half) {
       const int r = ra + half;
       float2* row = psi + b * rg.bstride + (long long)r * rg.pitch;
+      const float2* irow = psi_in + b * rg.bstride + (long long)r * rg.pitch;
       const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
 #pragma unroll
       for (int i = 0; i < N / (R1 * T); ++i)
 #pragma unroll
-        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? irow[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
       const int y = r % rg.ny, z = r / rg.ny;
       const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * z;
       // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2)
