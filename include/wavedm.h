@@ -196,6 +196,11 @@ int64_t wdm_launch_count(const wdm_ctx* ctx);
 /* out[2i], out[2i+1] = sin, cos of h[i] (|h| <= pi/2) as evaluated by the series
  * the precise phase form uses; device pointers, n values. */
 wdm_status wdm_selftest_sincos(const float* h_dev, float* out_dev, int64_t n);
+/* Runs one CTA that waits on an mbarrier nothing completes, through the bounded
+ * wait of the TMA-fed passes with a limit of limit_ns nanoseconds.  On return
+ * *bits holds the error bits the kernel recorded (1: wait abandoned) and
+ * *waited_ns how long it waited; the device stays usable. */
+wdm_status wdm_selftest_bounded_wait(int64_t limit_ns, int32_t* bits, int64_t* waited_ns);
 
 #ifdef __cplusplus
 }

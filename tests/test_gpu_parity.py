@@ -34,8 +34,12 @@ def _rand_c64(shape, seed):
     return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
 
 
+# nx >= 16 sends the y and z lines through the TMA-fed pass (16-line tiles,
+# the last one partial when 16 does not divide nx; 384 and 512 points take two
+# boxes per tile); nx < 16 keeps the register-tile pass
 FFT_SHAPES = [(8, 8, 8), (16, 12, 24), (32, 32, 32), (48, 64, 96), (128, 128, 128), (192, 16, 8), (256, 8, 16),
-              (384, 8, 8), (512, 8, 8), (8, 384, 16), (8, 16, 384), (64, 96, 12)]
+              (384, 8, 8), (512, 8, 8), (8, 384, 16), (8, 16, 384), (64, 96, 12), (16, 384, 8), (24, 8, 384),
+              (16, 512, 8), (48, 8, 512)]
 
 
 @pytest.mark.parametrize("n", FFT_SHAPES, ids=["x".join(map(str, s)) for s in FFT_SHAPES])
@@ -255,3 +259,21 @@ def test_series_sincos_error_bound(wdm, torch_cuda):
     assert np.max(np.abs(sc[:, 1] - c_ref)) <= 1.2e-7
     near1 = np.abs(c_ref) >= 0.7
     assert np.max(np.abs(sc[near1, 1] - c_ref[near1]) / ulp_c[near1]) <= 2.0
+
+
+def test_bounded_wait_runs_out_and_device_stays_usable(wdm, torch_cuda):
+    """A wait on an mbarrier that nothing completes gives up after its limit,
+    reports WDM_DEVERR_TMA_WAIT to the host and leaves the context usable."""
+    import ctypes as C
+
+    lib = wdm._abi.load()
+    bits, waited = C.c_int32(0), C.c_int64(0)
+    assert lib.wdm_selftest_bounded_wait(2_000_000, C.byref(bits), C.byref(waited)) == 0
+    assert bits.value == 1
+    assert 2_000_000 <= waited.value < 1_000_000_000
+    x = _rand_c64((16, 16, 32), 7)
+    with wdm.SPEContext((32, 16, 16), (1.0, 1.0, 1.0)) as ctx:
+        d = torch_cuda.from_numpy(x).cuda()
+        got = ctx.fft3d(d).cpu().numpy()
+    ref = np.fft.fftn(x.astype(np.complex128))
+    assert spe.rel_l2(got, ref) < 2e-6

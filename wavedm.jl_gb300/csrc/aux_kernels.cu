@@ -1,5 +1,6 @@
 // Auxiliary kernels: density output, FP64 diagnostics reductions, CIC.
 #include "aux_kernels.cuh"
+#include "tma.cuh"
 #include "wdm_math.cuh"
 
 namespace wdm {
@@ -41,6 +42,30 @@ cudaError_t launch_adj_seed(const float2* psi, const float* rho_t, float2* lam, 
   long long blocks = (n + 255) / 256;
   if (blocks > 608) blocks = 608;
   k_adj_seed<<<dim3((unsigned)blocks, batch), 256, 0, st>>>(psi, rho_t, lam, n, dV, loss);
+  return cudaGetLastError();
+}
+
+// One CTA waits on an mbarrier phase that nothing completes (no arrival, no
+// copy), through the same bounded wait the TMA line passes use; it records
+// WDM_DEVERR_TMA_WAIT in out[0] and the nanoseconds it waited in out[1].
+__global__ void k_bounded_wait_probe(unsigned long long limit_ns, unsigned long long* out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const unsigned long long t0 = globaltimer_ns();
+  const bool landed = mbar_wait_bounded(&bar, 0u, limit_ns);
+  const bool all = __syncthreads_and(landed);
+  if (threadIdx.x == 0) {
+    out[0] = all ? 0ull : (unsigned long long)WDM_DEVERR_TMA_WAIT;
+    out[1] = globaltimer_ns() - t0;
+  }
+}
+
+cudaError_t launch_bounded_wait_probe(unsigned long long limit_ns, unsigned long long* out, cudaStream_t st) {
+  k_bounded_wait_probe<<<1, 128, 0, st>>>(limit_ns, out);
   return cudaGetLastError();
 }
 

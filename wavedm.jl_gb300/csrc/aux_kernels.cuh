@@ -36,6 +36,8 @@ cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t
 // loss[b] += sum (|psi|^2 - rho_t)^2 dV (FP64), per batch item of n cells.
 cudaError_t launch_adj_seed(const float2* psi, const float* rho_t, float2* lam, long long n, int batch, double dV,
                             double* loss, cudaStream_t st);
+// bounded mbarrier wait that runs out (self-test): out[0] error bits, out[1] ns waited
+cudaError_t launch_bounded_wait_probe(unsigned long long limit_ns, unsigned long long* out, cudaStream_t st);
 // out[2i], out[2i+1] = series sin, cos of h[i] (wdm_math.cuh), for self-tests
 cudaError_t launch_sincos_half(const float* h, float* out, long long n, cudaStream_t st);
 // shift[b] = mean over item b of |data|^2 (complex_in) or of data (float), + add

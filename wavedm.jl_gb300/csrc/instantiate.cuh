@@ -40,11 +40,52 @@ template <int N>
 struct Launch {
   static constexpr int NT = threads_for<N>();
 
+  // Tensor map of the lines of g (null view: false).
+  static bool line_map(CUtensorMap* map, const float2* data, const LineGeom& g, int batch) {
+    using TT = TmaTile<N>;
+    if (g.axis != 1 && g.axis != 2) return false;
+    if (g.nxa < LINES || g.rows <= 0) return false;  // the box stays inside the tensor along x
+    const uint64_t e = sizeof(float2);
+    uint64_t dims[4], strides[3];
+    uint32_t box[4];
+    dims[0] = (uint64_t)g.nxa;
+    dims[3] = (uint64_t)batch;
+    strides[0] = (uint64_t)g.pitch * e;
+    strides[2] = (uint64_t)g.bstride * e;
+    if (g.axis == 1) {  // [batch][rows][N][pitch]
+      dims[1] = N;
+      dims[2] = (uint64_t)g.rows;
+      strides[1] = (uint64_t)g.pitch * N * e;
+      box[0] = LINES, box[1] = TT::BOXP, box[2] = 1, box[3] = 1;
+    } else {  // [batch][N][rows][pitch]
+      dims[1] = (uint64_t)g.rows;
+      dims[2] = N;
+      strides[1] = (uint64_t)g.pitch * g.rows * e;
+      box[0] = LINES, box[1] = 1, box[2] = TT::BOXP, box[3] = 1;
+    }
+    return encode_map_c64(map, data, dims, strides, box);
+  }
+
   // persistent line pass: one wave of resident CTAs walking all tiles
   template <int MODE, class Op>
   static cudaError_t lpipe(float2* data, const LineGeom& g, const float4* tw, const Op& op, int batch,
                            cudaStream_t st) {
     if (g.nlines <= 0 || batch <= 0) return cudaSuccess;
+#if !defined(WDM_LINE_PIPELINE) && !defined(WDM_LINE_TILE)
+    {
+      CUtensorMap map;
+      if (line_map(&map, data, g, batch)) {
+        constexpr size_t SMEM = ltma_smem_bytes<N, MODE>();
+        cudaError_t e;
+        if ((e = prep_once<k_lfft_tma<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
+        const long long tiles = (long long)g.rows * ((g.nxa + LINES - 1) / LINES) * batch;
+        const long long cap = (long long)resident_ctas<k_lfft_tma<N, MODE, Op>>(NT, SMEM) * sm_count();
+        const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
+        k_lfft_tma<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, map, g, tw, op, batch);
+        return cudaGetLastError();
+      }
+    }
+#endif
 #ifndef WDM_LINE_PIPELINE
     {
       constexpr size_t SMEM = ltile_smem_bytes<N, MODE>();

@@ -16,6 +16,7 @@
 //   P8 k_lfft<inv>    H, y axis
 #pragma once
 #include "fft_engine.cuh"
+#include "tma.cuh"
 #include "wdm_math.cuh"
 
 namespace wdm {
@@ -48,6 +49,13 @@ struct LineGeom {
   long long outer;    // element stride between successive groups of nxa lines
   long long pstride;  // element stride between points of one line
   long long bstride;  // element stride between batch items
+  // tensor-map view for the TMA-fed pass: the array is [batch][d2][d1][pitch]
+  // with the lines along d1 (axis 1) or d2 (axis 2); `rows` counts the other
+  // of d1/d2, so a batch item holds rows * ceil(nxa / LINES) tiles
+  int axis = 0;          // 1: lines along y, 2: lines along z, 0: no tensor-map view
+  int rows = 0;          // groups of nxa lines per batch item
+  long long pitch = 0;   // element stride along y (row pitch)
+  int* err = nullptr;    // device-visible error word (bounded waits), may be null
 };
 
 struct RowGeom {
@@ -291,6 +299,131 @@ k_lfft_tile(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
 template <int N, int MODE>
 __host__ __device__ constexpr size_t ltile_smem_bytes() {
   return sizeof(float2) * (size_t)(2 * (MODE == 2 ? 2 : 1) * N + N * LPITCH);
+}
+
+// TMA-fed persistent line pass.  A tile is LINES lines that are neighbours
+// along x (one 128-byte row of the box per point), so the box lands in shared
+// memory as a dense [N][LINES] array: the layout stage_read expects with a
+// pitch of LINES, conflict-free because each half-warp touches one 128-byte
+// row.  Each CTA keeps two tile slots: the bulk tensor copy of its next tile
+// is in flight while the current one is transformed in place in its own slot
+// and stored from registers, so the loads are never behind the arithmetic.
+// One thread issues the copies; every wait on a slot's mbarrier is bounded,
+// and a CTA that gives up records WDM_DEVERR_TMA_WAIT, drains its copies
+// (bounded again) and exits.
+template <int N>
+struct TmaTile {
+  static constexpr int BOXP = N <= 256 ? N : N / 2;  // points per box (box extents are <= 256)
+  static constexpr int NBOX = N / BOXP;
+  static constexpr unsigned BYTES = (unsigned)(N * LINES * sizeof(float2));
+};
+
+template <int N, int MODE>
+__host__ __device__ constexpr size_t ltma_smem_bytes() {
+  // two tile slots, the twiddle table(s), two mbarriers
+  return 2 * (size_t)TmaTile<N>::BYTES + sizeof(float4) * (MODE == 2 ? 2 : 1) * N + 2 * sizeof(uint64_t);
+}
+
+template <int N>
+__device__ __forceinline__ void ltma_issue(const CUtensorMap* map, float2* slot, uint64_t* bar, const LineGeom& g,
+                                           long long tile, int tx) {
+  using TT = TmaTile<N>;
+  const long long per_item = (long long)g.rows * tx;
+  const int b = (int)(tile / per_item);
+  const int rem = (int)(tile - (long long)b * per_item);
+  const int row = rem / tx, x0 = (rem - row * tx) * LINES;
+  mbar_expect_tx(bar, TT::BYTES);
+#pragma unroll
+  for (int q = 0; q < TT::NBOX; ++q) {
+    if (g.axis == 1)
+      tma_load_4d(slot + q * TT::BOXP * LINES, map, bar, x0, q * TT::BOXP, row, b);
+    else
+      tma_load_4d(slot + q * TT::BOXP * LINES, map, bar, x0, row, q * TT::BOXP, b);
+  }
+}
+
+template <int N>
+__host__ __device__ constexpr int ltma_min_blocks() {
+  return ltma_smem_bytes<N, 2>() * 2 <= 220 * 1024 ? (threads_for<N>() * 2 <= 1024 ? 2 : 1) : 1;
+}
+
+template <int N, int MODE, class Op>
+__global__ void __launch_bounds__(threads_for<N>(), ltma_min_blocks<N>())
+k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, LineGeom g,
+           const float4* __restrict__ twg, Op op, int batch) {
+  using P = Plan<N>;
+  using TT = TmaTile<N>;
+  constexpr int T = P::T;
+  using Rad = typename P::Fwd;
+  using Rev = typename Reverse<Rad>::type;
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
+  constexpr int NTAB = MODE == 2 ? 2 : 1;
+  extern __shared__ __align__(1024) unsigned char lsm[];
+  float2* slots = reinterpret_cast<float2*>(lsm);
+  float4* tw = reinterpret_cast<float4*>(lsm + 2 * TT::BYTES);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(lsm + 2 * TT::BYTES + sizeof(float4) * NTAB * N);
+  const int tid = threadIdx.x;
+  const int l = tid % LINES, t = tid / LINES;
+  const int tx = (g.nxa + LINES - 1) / LINES;
+  const long long per_item = (long long)g.rows * tx;
+  const long long total = per_item * batch;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
+  __syncthreads();
+  long long tile = blockIdx.x;
+  if (tid == 0 && tile < total) ltma_issue<N>(&map, slots, &bar[0], g, tile, tx);
+  int it = 0;
+  unsigned pending = tile < total ? 1u : 0u;  // bit s: slot s has a copy in flight
+  for (; tile < total; tile += gridDim.x, ++it) {
+    const int cur = it & 1;
+    const long long nxt = tile + gridDim.x;
+    if (nxt < total) {
+      if (tid == 0) ltma_issue<N>(&map, slots + (cur ^ 1) * N * LINES, &bar[cur ^ 1], g, nxt, tx);
+      pending |= 1u << (cur ^ 1);
+    }
+    const bool landed = mbar_wait_bounded(&bar[cur], (unsigned)(it >> 1) & 1u);
+    if (!__syncthreads_and(landed)) {
+      if (tid == 0 && g.err) atomicOr(g.err, WDM_DEVERR_TMA_WAIT);
+      // drain: the slot that timed out and the look-ahead copy, each bounded
+      const bool d0 = mbar_wait_bounded(&bar[cur], (unsigned)(it >> 1) & 1u);
+      const bool d1 = !((pending >> (cur ^ 1)) & 1u) || mbar_wait_bounded(&bar[cur ^ 1], (unsigned)((it + 1) >> 1) & 1u);
+      if (tid == 0 && g.err && !(d0 && d1)) atomicOr(g.err, WDM_DEVERR_TMA_DRAIN);
+      return;
+    }
+    pending &= ~(1u << cur);
+    float2* s = slots + cur * N * LINES;
+    const int b = (int)(tile / per_item);
+    const int rem = (int)(tile - (long long)b * per_item);
+    const int row = rem / tx, x = (rem - row * tx) * LINES + l;
+    const bool ok = x < g.nxa;
+    const int line = row * g.nxa + (ok ? x : 0);
+    float2* base = data + b * g.bstride + line_base(g, line);
+    float2 v[N / T];
+    stage_read<N, T, R1, LINES>(s, v, t, l);
+    if constexpr (MODE == 1) {
+      run_stages<N, T, LINES, true>(Rad{}, v, s, tw, t, l);
+    } else {
+      run_stages<N, T, LINES, false>(Rad{}, v, s, tw, t, l);
+    }
+    if constexpr (MODE == 2) {
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], line, slot_pos<N, T, RS>(t, i, k), b);
+      run_stages<N, T, LINES, true>(Rev{}, v, s, tw + N, t, l);
+      lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
+    } else {
+      lines_store<N, RS>(v, base, g.pstride, ok, t);
+    }
+    // the slot's generic reads and writes are done before the copy of
+    // tile + 2 gridDim overwrites it
+    fence_proxy_async_smem();
+    __syncthreads();
+  }
 }
 
 // ----------------------------------------------------------------------------

@@ -112,7 +112,7 @@ struct wdm_ctx {
   float* T6b = nullptr;             // per-batch-item tidal tensors
   std::vector<double> tide;         // host schedule rows of 6
   int tide_on = 0;
-  int* flag = nullptr;              // device non-finite flag
+  int* flag = nullptr;              // device words: [0] non-finite psi, [1] abandoned-wait bits
   float* scratch_f = nullptr;       // float field scratch [batch][ncell]
   float2* scratch_h = nullptr;      // half-spectrum scratch
   double* red = nullptr;            // reduction partials
@@ -346,6 +346,10 @@ static LineGeom lines_y(const wdm_ctx* c, int xext, long long bstride) {
   g.outer = (long long)c->d.ny * xext;
   g.pstride = xext;
   g.bstride = bstride;
+  g.axis = 1;
+  g.rows = c->d.nz;
+  g.pitch = xext;
+  g.err = c->flag + 1;
   return g;
 }
 
@@ -356,6 +360,10 @@ static LineGeom lines_z(const wdm_ctx* c, int xext, long long bstride) {
   g.outer = xext;
   g.pstride = (long long)c->d.ny * xext;
   g.bstride = bstride;
+  g.axis = 2;
+  g.rows = c->d.ny;
+  g.pitch = xext;
+  g.err = c->flag + 1;
   return g;
 }
 
@@ -498,10 +506,14 @@ static wdm_status drift_yz(wdm_ctx* c, double dt, float sign = 1.f, float2* data
 
 static wdm_status sync_and_check(wdm_ctx* c) {
   WDM_CU(c, cudaStreamSynchronize(c->st));
-  int flag = 0;
-  WDM_CU(c, cudaMemcpy(&flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost));
-  if (fault_injected("nonfinite")) flag = 1;
-  if (flag) return fail(c, WDM_ERR_NONFINITE, "psi became non-finite (NaN/Inf density)");
+  int flag[2] = {0, 0};
+  WDM_CU(c, cudaMemcpy(flag, c->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag[1])
+    return fail(c, WDM_ERR_CUDA,
+                "a line pass abandoned a bounded wait for its TMA tile (device error bits " +
+                    std::to_string(flag[1]) + "); psi is stale until wdm_set_psi");
+  if (fault_injected("nonfinite")) flag[0] = 1;
+  if (flag[0]) return fail(c, WDM_ERR_NONFINITE, "psi became non-finite (NaN/Inf density)");
   return WDM_OK;
 }
 
@@ -634,8 +646,8 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   if ((s = dalloc(c, &c->mx, d->nx)) != WDM_OK) return bail(s);
   if ((s = dalloc(c, &c->my, d->ny)) != WDM_OK) return bail(s);
   if ((s = dalloc(c, &c->mz, d->nz)) != WDM_OK) return bail(s);
-  if ((s = dalloc(c, &c->flag, 1)) != WDM_OK) return bail(s);
-  if ((e = cudaMemsetAsync(c->flag, 0, sizeof(int), c->st)) != cudaSuccess) {
+  if ((s = dalloc(c, &c->flag, 2)) != WDM_OK) return bail(s);
+  if ((e = cudaMemsetAsync(c->flag, 0, 2 * sizeof(int), c->st)) != cudaSuccess) {
     cuda_fail(c, e, "memset flag");
     return bail(WDM_ERR_CUDA);
   }
@@ -659,7 +671,7 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
 wdm_status wdm_set_psi(wdm_ctx* c, const void* psi, int32_t where) {
   if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
   WDM_TRY(copy_in(c, c->psi, psi, sizeof(float2) * c->ncell * c->d.batch, where));
-  WDM_CU(c, cudaMemsetAsync(c->flag, 0, sizeof(int), c->st));
+  WDM_CU(c, cudaMemsetAsync(c->flag, 0, 2 * sizeof(int), c->st));
   WDM_CU(c, cudaStreamSynchronize(c->st));
   WDM_TRY(update_shift(c));
   c->have_psi = 1;
@@ -983,6 +995,22 @@ wdm_status wdm_selftest_sincos(const float* h, float* out, int64_t n) {
   cudaError_t e = launch_sincos_half(h, out, n, nullptr);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return fail(nullptr, WDM_ERR_CUDA, std::string("wdm_selftest_sincos: ") + cudaGetErrorString(e));
+  return WDM_OK;
+}
+
+wdm_status wdm_selftest_bounded_wait(int64_t limit_ns, int32_t* bits, int64_t* waited_ns) {
+  if (!bits || !waited_ns || limit_ns < 0 || limit_ns > 10000000000LL)
+    return fail(nullptr, WDM_ERR_INVALID, "wdm_selftest_bounded_wait: bad arguments (limit 0..1e10 ns)");
+  unsigned long long* d = nullptr;
+  unsigned long long h[2] = {0, 0};
+  cudaError_t e = cudaMalloc((void**)&d, sizeof(h));
+  if (e == cudaSuccess) e = launch_bounded_wait_probe((unsigned long long)limit_ns, d, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  if (e != cudaSuccess)
+    return fail(nullptr, WDM_ERR_CUDA, std::string("wdm_selftest_bounded_wait: ") + cudaGetErrorString(e));
+  *bits = (int32_t)h[0];
+  *waited_ns = (int64_t)h[1];
   return WDM_OK;
 }
 
