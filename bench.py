@@ -62,13 +62,21 @@ class ClockSampler:
         self.f = None
 
     def start(self):
+        """Start sampling every 50 ms; returns once the first sample is in, so the
+        samples cover a timed region that starts afterwards."""
         try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:
@@ -185,6 +193,7 @@ def run_native(args, rank, world):
         nb = psi0.nbytes
         e2e = {"value": ne * world / el, "unit": "steps/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ne, "calls_per_step": ["wdm_set_psi(host)", "wdm_step(1)", "wdm_get_psi(host)"]}
+    sched = ctx.line_schedule()
     ctx.close()
 
     # roofline of the dominant pass
@@ -222,6 +231,7 @@ def run_native(args, rank, world):
                            "GBps": round(B_ALG_PER_CELL * ncell * value / world / 1e9, 1),
                            "frac_of_peak": round(B_ALG_PER_CELL * ncell * value / world / 1e9 / peak, 4)},
         "passes": passes,
+        "line_schedule": sched,
         "gpu_launches": int(launches),
         "e2e": e2e,
         "clocks": clk,
@@ -274,12 +284,19 @@ def run_ensemble(args, rank, world):
         torch.distributed.barrier()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
     clocks.start()
+    gs = torch.cuda.ExternalStream(ens.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = ens.launch_count
-    t0 = time.perf_counter()
-    ens.step(K, dts)  # graph replay; returns when done
-    el = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    ev0.record(gs)
+    ens.step(K, dts, sync=False)  # one graph replay on the group's stream
+    ev1.record(gs)
+    torch.cuda.synchronize()
+    el = ev0.elapsed_time(ev1) / 1e3
     launches = ens.launch_count - l0
     clk = clocks.stop()
+    if not all(c.is_finite() for c in ctxs):
+        raise RuntimeError("ensemble state became non-finite")
     if world > 1:
         t = torch.tensor([el], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -458,7 +475,7 @@ def ensemble_cpu_baseline(budget_s):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--workload", type=int, default=3)

@@ -119,6 +119,11 @@ wdm_status wdm_group_create(wdm_ctx* const* members, int32_t n, wdm_group** out)
 wdm_status wdm_group_destroy(wdm_group* g);
 /* nsteps steps of every member, member i with time step dts[i] */
 wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode);
+/* the same, returning once the graph is enqueued on the group's stream (check
+ * the members with wdm_check_finite after synchronising the stream) */
+wdm_status wdm_group_step_async(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode);
+/* the group's cudaStream_t */
+void* wdm_group_stream(const wdm_group* g);
 /* kernel launches executed by the group's graph replays so far */
 int64_t wdm_group_launch_count(const wdm_group* g);
 
@@ -186,6 +191,12 @@ wdm_status wdm_set_profiling(wdm_ctx* ctx, int32_t on);
 /* for pass p < WDM_NPASS: launches, summed milliseconds and algorithmic bytes
  * (one read + one write of every operand) of one launch, since profiling on */
 wdm_status wdm_get_profile(wdm_ctx* ctx, int64_t* launches, double* ms, double* bytes_per_launch);
+/* Line-pass schedule chosen by the autotuner when the context was created,
+ * for the passes psi-y, psi-z, H-y, H-z in that order: impl[k] = 0 for the
+ * TMA-fed persistent pass, 1 for the register-tile pass; ms[2k], ms[2k+1] the
+ * best timed milliseconds of the two (-1: not timed, e.g. forced through the
+ * environment variable WDM_LINE_IMPL=tma|tile). */
+wdm_status wdm_get_line_schedule(const wdm_ctx* ctx, int32_t impl[4], double ms[8]);
 /* number of passes and the name of pass p */
 int32_t wdm_num_passes(void);
 const char* wdm_pass_name(int32_t p);

@@ -277,3 +277,37 @@ def test_bounded_wait_runs_out_and_device_stays_usable(wdm, torch_cuda):
         got = ctx.fft3d(d).cpu().numpy()
     ref = np.fft.fftn(x.astype(np.complex128))
     assert spe.rel_l2(got, ref) < 2e-6
+
+
+@pytest.mark.parametrize("n", [(32, 24, 16), (48, 64, 96), (24, 16, 384)])
+def test_line_pass_implementations_agree(wdm, n, monkeypatch):
+    """The TMA-fed and the register-tile line passes do the same arithmetic, so a
+    run forced onto either one gives the same psi; the autotuner only picks speed."""
+    nx, ny, nz = n
+    L = (4.0, 3.0, 5.0)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    rng = np.random.default_rng(3)
+    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2)) * np.exp(1j * rng.uniform(0, 1, (nz, ny, nx)))).astype(np.complex64)
+    out = {}
+    for impl in ("tma", "tile"):
+        monkeypatch.setenv("WDM_LINE_IMPL", impl)
+        with wdm.SPEContext(n, L, poisson_coeff=2.0) as ctx:
+            sched = ctx.line_schedule()
+            assert all(v["impl"] == impl for v in sched.values())
+            ctx.set_psi(psi0)
+            ctx.step(3, 0.01)
+            out[impl] = ctx.get_psi()
+    assert np.array_equal(out["tma"], out["tile"])
+
+
+def test_autotuner_reports_a_schedule(wdm, monkeypatch):
+    monkeypatch.delenv("WDM_LINE_IMPL", raising=False)
+    with wdm.SPEContext((64, 64, 64), (1.0, 1.0, 1.0)) as ctx:
+        sched = ctx.line_schedule()
+    assert set(sched) == {"psi_y", "psi_z", "h_y", "h_z"}
+    for v in sched.values():
+        assert v["impl"] in ("tma", "tile")
+        assert 0 < v["ms_tma"] < 1e3 and 0 < v["ms_tile"] < 1e3
+        faster = "tile" if v["ms_tile"] < 0.97 * v["ms_tma"] else "tma"
+        assert v["impl"] == faster

@@ -76,11 +76,14 @@ SIGNATURES = [
     ("wdm_launch_count", _i64, [_vp]),
     ("wdm_selftest_sincos", _i32, [_vp, _vp, _i64]),
     ("wdm_selftest_bounded_wait", _i32, [_i64, C.POINTER(_i32), C.POINTER(_i64)]),
+    ("wdm_get_line_schedule", _i32, [_vp, _vp, _vp]),
     ("wdm_step_graph", _i32, [_vp, _i32, _d, _i32]),
     ("wdm_adjoint", _i32, [_vp, _i32, _d, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
     ("wdm_group_create", _i32, [_vp, _i32, C.POINTER(_vp)]),
     ("wdm_group_destroy", _i32, [_vp]),
     ("wdm_group_step", _i32, [_vp, _i32, _vp, _i32]),
+    ("wdm_group_step_async", _i32, [_vp, _i32, _vp, _i32]),
+    ("wdm_group_stream", _vp, [_vp]),
     ("wdm_group_launch_count", _i64, [_vp]),
 ]
 

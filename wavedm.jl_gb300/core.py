@@ -229,6 +229,18 @@ class SPEContext:
         return {self.lib.wdm_pass_name(p).decode(): dict(launches=int(la[p]), ms=float(ms[p]),
                                                           bytes_per_launch=float(by[p])) for p in range(n)}
 
+    LINE_PASSES = ("psi_y", "psi_z", "h_y", "h_z")
+    LINE_IMPLS = ("tma", "tile")
+
+    def line_schedule(self):
+        """{line pass: dict(impl, ms_tma, ms_tile)} as chosen by the autotuner at creation."""
+        impl = np.zeros(4, np.int32)
+        ms = np.zeros(8, np.float64)
+        self._check(self.lib.wdm_get_line_schedule(self.handle, C.c_void_p(impl.ctypes.data),
+                                                   C.c_void_p(ms.ctypes.data)))
+        return {name: dict(impl=self.LINE_IMPLS[int(impl[k])], ms_tma=float(ms[2 * k]), ms_tile=float(ms[2 * k + 1]))
+                for k, name in enumerate(self.LINE_PASSES)}
+
     @property
     def launch_count(self):
         return int(self.lib.wdm_launch_count(self.handle))
@@ -250,9 +262,16 @@ class Ensemble:
         check(self.lib.wdm_group_create(arr, len(self.members), C.byref(h)))
         self._h = h
 
-    def step(self, nsteps, dts, mode="strang"):
+    def step(self, nsteps, dts, mode="strang", sync=True):
+        """Advance every member; sync=False returns once the graph is enqueued on self.stream."""
         d = np.ascontiguousarray(np.broadcast_to(np.asarray(dts, np.float64), (len(self.members),)))
-        check(self.lib.wdm_group_step(self._h, int(nsteps), C.c_void_p(d.ctypes.data), _abi.STEP_MODES[mode]))
+        fn = self.lib.wdm_group_step if sync else self.lib.wdm_group_step_async
+        check(fn(self._h, int(nsteps), C.c_void_p(d.ctypes.data), _abi.STEP_MODES[mode]))
+
+    @property
+    def stream(self):
+        """The group's cudaStream_t (as an integer handle)."""
+        return int(self.lib.wdm_group_stream(self._h) or 0)
 
     @property
     def launch_count(self):

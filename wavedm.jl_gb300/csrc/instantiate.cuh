@@ -74,7 +74,7 @@ struct Launch {
 #if !defined(WDM_LINE_PIPELINE) && !defined(WDM_LINE_TILE)
     {
       CUtensorMap map;
-      if (line_map(&map, data, g, batch)) {
+      if (g.impl == LINE_IMPL_TMA && line_map(&map, data, g, batch)) {
         constexpr size_t SMEM = ltma_smem_bytes<N, MODE>();
         cudaError_t e;
         if ((e = prep_once<k_lfft_tma<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
@@ -82,19 +82,14 @@ struct Launch {
         const long long cap = (long long)resident_ctas<k_lfft_tma<N, MODE, Op>>(NT, SMEM) * sm_count();
         const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
         k_lfft_tma<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, map, g, tw, op, batch);
+        ++tl_kernel_launches;
         return cudaGetLastError();
       }
     }
 #endif
 #ifndef WDM_LINE_PIPELINE
-    {
-      constexpr size_t SMEM = ltile_smem_bytes<N, MODE>();
-      cudaError_t e;
-      if ((e = prep_once<k_lfft_tile<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
-      k_lfft_tile<N, MODE, Op><<<dim3((g.nlines + LINES - 1) / LINES, batch), NT, SMEM, st>>>(data, g, tw, op);
-      return cudaGetLastError();
-    }
-#endif
+    return ltile<MODE>(data, g, tw, op, batch, st);
+#else
     constexpr size_t SMEM = lpipe_smem_bytes<N, MODE>();
     cudaError_t e;
     if ((e = prep_once<k_lfft_pipe<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
@@ -102,6 +97,20 @@ struct Launch {
     const long long cap = (long long)resident_ctas<k_lfft_pipe<N, MODE, Op>>(NT, SMEM) * sm_count();
     const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
     k_lfft_pipe<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, g, tw, op, batch);
+    ++tl_kernel_launches;
+    return cudaGetLastError();
+#endif
+  }
+
+  // one register tile of LINES lines per CTA (lines may straddle rows)
+  template <int MODE, class Op>
+  static cudaError_t ltile(float2* data, const LineGeom& g, const float4* tw, const Op& op, int batch,
+                           cudaStream_t st) {
+    constexpr size_t SMEM = ltile_smem_bytes<N, MODE>();
+    cudaError_t e;
+    if ((e = prep_once<k_lfft_tile<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
+    k_lfft_tile<N, MODE, Op><<<dim3((g.nlines + LINES - 1) / LINES, batch), NT, SMEM, st>>>(data, g, tw, op);
+    ++tl_kernel_launches;
     return cudaGetLastError();
   }
 
@@ -136,9 +145,11 @@ struct Launch {
     if (inv) {
       if ((e = prep_once<k_xw_fft<N, true>>(XSMEM)) != cudaSuccess) return e;
       k_xw_fft<N, true><<<gr, XNT, XSMEM, st>>>(data, rg, tw, scale, w);
+      ++tl_kernel_launches;
     } else {
       if ((e = prep_once<k_xw_fft<N, false>>(XSMEM)) != cudaSuccess) return e;
       k_xw_fft<N, false><<<gr, XNT, XSMEM, st>>>(data, rg, tw, scale, w);
+      ++tl_kernel_launches;
     }
     return cudaGetLastError();
   }
@@ -149,6 +160,7 @@ struct Launch {
     const dim3 gr = grid_x(rg, batch, &w);
     if ((e = prep_once<k_xw_inv_rho<N>>(XSMEM)) != cudaSuccess) return e;
     k_xw_inv_rho<N><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
+    ++tl_kernel_launches;
     return cudaGetLastError();
   }
   static cudaError_t x_kick(const float2* psi_in, float2* psi, const float2* H, const RowGeom& rg, long long hpitch,
@@ -160,9 +172,11 @@ struct Launch {
     if (fwd) {
       if ((e = prep_once<k_xw_kick<N, true>>(XSMEM)) != cudaSuccess) return e;
       k_xw_kick<N, true><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
+      ++tl_kernel_launches;
     } else {
       if ((e = prep_once<k_xw_kick<N, false>>(XSMEM)) != cudaSuccess) return e;
       k_xw_kick<N, false><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
+      ++tl_kernel_launches;
     }
     return cudaGetLastError();
   }
@@ -173,6 +187,7 @@ struct Launch {
     const dim3 gr = grid_x(rg, batch, &w);
     if ((e = prep_once<k_xw_c2r<N>>(XSMEM)) != cudaSuccess) return e;
     k_xw_c2r<N><<<gr, XNT, XSMEM, st>>>(H, out, rg, hpitch, hbstride, tw, w);
+    ++tl_kernel_launches;
     return cudaGetLastError();
   }
   static cudaError_t x_r2c(const float* in, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
@@ -182,6 +197,7 @@ struct Launch {
     const dim3 gr = grid_x(rg, batch, &w);
     if ((e = prep_once<k_xw_r2c<N>>(XSMEM)) != cudaSuccess) return e;
     k_xw_r2c<N><<<gr, XNT, XSMEM, st>>>(in, H, rg, hpitch, hbstride, tw, shift, w);
+    ++tl_kernel_launches;
     return cudaGetLastError();
   }
   // host: the four stage-major twiddle tables of this axis length (TW_TABLES x N)
@@ -208,6 +224,7 @@ struct Launch {
     const dim3 gr = grid_x(rg, batch, &w);
     if ((e = prep_once<k_xw_adj_kick<N>>(XSMEM)) != cudaSuccess) return e;
     k_xw_adj_kick<N><<<gr, XNT, XSMEM, st>>>(lam, H, Hmu, rg, hpitch, hbstride, tw, a, j, w);
+    ++tl_kernel_launches;
     return cudaGetLastError();
   }
   static cudaError_t adj_apply(float2* lam, const float2* Hmu, const RowGeom& rg, long long hpitch, long long hbstride,
@@ -218,9 +235,11 @@ struct Launch {
     if (fwd) {
       if ((e = prep_once<k_xw_adj_apply<N, true>>(XSMEM)) != cudaSuccess) return e;
       k_xw_adj_apply<N, true><<<gr, XNT, XSMEM, st>>>(lam, Hmu, rg, hpitch, hbstride, tw, j, w);
+      ++tl_kernel_launches;
     } else {
       if ((e = prep_once<k_xw_adj_apply<N, false>>(XSMEM)) != cudaSuccess) return e;
       k_xw_adj_apply<N, false><<<gr, XNT, XSMEM, st>>>(lam, Hmu, rg, hpitch, hbstride, tw, j, w);
+      ++tl_kernel_launches;
     }
     return cudaGetLastError();
   }

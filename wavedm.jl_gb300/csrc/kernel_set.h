@@ -7,6 +7,10 @@
 
 namespace wdm {
 
+// Kernels launched by this host thread through the KernelSet launchers (a
+// pass may take more than one launch); the API layer counts launches from it.
+extern thread_local long long tl_kernel_launches;
+
 struct KernelSet {
   int n;
   // strided lines (y or z axis), C2C in place

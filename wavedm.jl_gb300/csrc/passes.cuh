@@ -56,7 +56,13 @@ struct LineGeom {
   int rows = 0;          // groups of nxa lines per batch item
   long long pitch = 0;   // element stride along y (row pitch)
   int* err = nullptr;    // device-visible error word (bounded waits), may be null
+  int x0 = 0;            // x column of the first line (k-space operators see mx = x0 + column)
+  int impl = 0;          // LINE_IMPL_TMA or LINE_IMPL_TILE (chosen per pass by the autotuner)
 };
+
+// Implementations of a line pass: the TMA-fed persistent pass (used where the
+// array has a tensor-map view) and the one-register-tile-per-CTA pass.
+enum { LINE_IMPL_TMA = 0, LINE_IMPL_TILE = 1 };
 
 struct RowGeom {
   int nrows;          // rows per batch item (ny * nz)
@@ -71,7 +77,7 @@ __device__ __forceinline__ long long line_base(const LineGeom& g, int line) {
 
 // ----------------------------------------------------------------------------
 // k-space operators applied between the forward and inverse transforms of a
-// fused pass.  `line` indexes (mx + nxa * my), `pos` is mz, `b` the batch item.
+// fused pass at mode (mx, my, pos = mz) of batch item b.
 // ----------------------------------------------------------------------------
 // Exact error of the FP32 sum s = a + b (Knuth two-sum).
 __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
@@ -99,11 +105,9 @@ struct DriftOp {
   float half_dt;
   float scale;
   float sign;             // +1: exp(-i k^2 dt/2); -1: its conjugate (the drift adjoint)
-  int nxa;
   int precise;
   long long tab_bstride;  // per-batch-item stride of the phase tables (0 = shared)
-  __device__ __forceinline__ float2 operator()(float2 v, int line, int pos, int b) const {
-    const int mx = line % nxa, my = line / nxa;
+  __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int b) const {
     if (precise) {
       const long long o = b * tab_bstride;
       const float2 tx = cx[o + mx], ty = cy[o + my], tz = cz[o + pos];
@@ -130,9 +134,7 @@ struct PoissonOp {
   const float* ky2;
   const float* kz2;
   float coef;  // -c / (nx ny nz)
-  int nxa;
-  __device__ __forceinline__ float2 operator()(float2 v, int line, int pos, int) const {
-    const int mx = line % nxa, my = line / nxa;
+  __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int) const {
     const float k2 = kx2[mx] + ky2[my] + kz2[pos];
     const float f = (k2 > 0.f) ? coef / k2 : 0.f;
     return make_float2(v.x * f, v.y * f);
@@ -234,10 +236,11 @@ k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
     float2* base = data + b * g.bstride + (ok ? line_base(g, line) : 0);
     if constexpr (MODE == 2) {
       const int lc = ok ? line : 0;
+      const int mx = g.x0 + lc % g.nxa, my = lc / g.nxa;
 #pragma unroll
       for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], lc, slot_pos<N, T, RS>(t, i, k), b);
+        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), b);
       run_stages<N, T, LBUF, true>(Rev{}, v, s, tw + N, t, l);
       lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
     } else {
@@ -250,7 +253,7 @@ k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
 }
 
 struct NoOp {
-  __device__ __forceinline__ float2 operator()(float2 v, int, int, int) const { return v; }
+  __device__ __forceinline__ float2 operator()(float2 v, int, int, int, int) const { return v; }
 };
 
 // One tile of LINES lines per CTA, loaded straight into registers (every
@@ -285,10 +288,11 @@ k_lfft_tile(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
   }
   if constexpr (MODE == 2) {
     const int lc = ok ? line : 0;
+    const int mx = g.x0 + lc % g.nxa, my = lc / g.nxa;
 #pragma unroll
     for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], lc, slot_pos<N, T, RS>(t, i, k), blockIdx.y);
+      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), blockIdx.y);
     run_stages<N, T, LPITCH, true>(Rev{}, v, s, tw + N, t, l);
     lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
   } else {
@@ -364,6 +368,8 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
   uint64_t* bar = reinterpret_cast<uint64_t*>(lsm + 2 * TT::BYTES + sizeof(float4) * NTAB * N);
   const int tid = threadIdx.x;
   const int l = tid % LINES, t = tid / LINES;
+  // tiles of 16 columns; when 16 does not divide nxa the last tile of a row
+  // reaches past the tensor (zero-filled by the copy, not stored)
   const int tx = (g.nxa + LINES - 1) / LINES;
   const long long per_item = (long long)g.rows * tx;
   const long long total = per_item * batch;
@@ -376,20 +382,20 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
   __syncthreads();
   long long tile = blockIdx.x;
   if (tid == 0 && tile < total) ltma_issue<N>(&map, slots, &bar[0], g, tile, tx);
-  int it = 0;
   unsigned pending = tile < total ? 1u : 0u;  // bit s: slot s has a copy in flight
-  for (; tile < total; tile += gridDim.x, ++it) {
+  for (int it = 0; tile < total; tile += gridDim.x, ++it) {
     const int cur = it & 1;
+    const unsigned par = (unsigned)(it >> 1) & 1u;  // slot cur's k-th use completes phase k
     const long long nxt = tile + gridDim.x;
     if (nxt < total) {
       if (tid == 0) ltma_issue<N>(&map, slots + (cur ^ 1) * N * LINES, &bar[cur ^ 1], g, nxt, tx);
       pending |= 1u << (cur ^ 1);
     }
-    const bool landed = mbar_wait_bounded(&bar[cur], (unsigned)(it >> 1) & 1u);
+    const bool landed = mbar_wait_bounded(&bar[cur], par);
     if (!__syncthreads_and(landed)) {
       if (tid == 0 && g.err) atomicOr(g.err, WDM_DEVERR_TMA_WAIT);
       // drain: the slot that timed out and the look-ahead copy, each bounded
-      const bool d0 = mbar_wait_bounded(&bar[cur], (unsigned)(it >> 1) & 1u);
+      const bool d0 = mbar_wait_bounded(&bar[cur], par);
       const bool d1 = !((pending >> (cur ^ 1)) & 1u) || mbar_wait_bounded(&bar[cur ^ 1], (unsigned)((it + 1) >> 1) & 1u);
       if (tid == 0 && g.err && !(d0 && d1)) atomicOr(g.err, WDM_DEVERR_TMA_DRAIN);
       return;
@@ -400,8 +406,8 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
     const int rem = (int)(tile - (long long)b * per_item);
     const int row = rem / tx, x = (rem - row * tx) * LINES + l;
     const bool ok = x < g.nxa;
-    const int line = row * g.nxa + (ok ? x : 0);
-    float2* base = data + b * g.bstride + line_base(g, line);
+    const int mx = ok ? x : 0;
+    float2* base = data + b * g.bstride + (long long)row * g.outer + mx;
     float2 v[N / T];
     stage_read<N, T, R1, LINES>(s, v, t, l);
     if constexpr (MODE == 1) {
@@ -413,7 +419,7 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
 #pragma unroll
       for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], line, slot_pos<N, T, RS>(t, i, k), b);
+        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], g.x0 + mx, row, slot_pos<N, T, RS>(t, i, k), b);
       run_stages<N, T, LINES, true>(Rev{}, v, s, tw + N, t, l);
       lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
     } else {

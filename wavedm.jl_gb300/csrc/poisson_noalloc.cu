@@ -206,7 +206,6 @@ extern "C" wdm_status wdm_poisson_noalloc(const float* rho, float* phi, int32_t 
   po.ky2 = k2[1];
   po.kz2 = k2[2];
   po.coef = (float)(-poisson_coeff / ((double)nx * ny * nz));
-  po.nxa = nxh;
   if (e == cudaSuccess) e = launch_mean_shift(rho, false, ncell, 1, sums, shift, 0.0, st);
   if (e == cudaSuccess) e = ks[0]->x_r2c(rho, H, rg, nxh, nhalf, tw[0], shift, 1, st);
   if (e == cudaSuccess) e = ks[1]->lfft(H, gy, tw[1], false, 1, st);

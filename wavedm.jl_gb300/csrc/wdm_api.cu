@@ -5,7 +5,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/wavedm.h"
@@ -13,6 +16,8 @@
 #include "kernel_set.h"
 
 namespace wdm {
+thread_local long long tl_kernel_launches = 0;
+
 const KernelSet* ks_8();
 const KernelSet* ks_12();
 const KernelSet* ks_16();
@@ -88,11 +93,16 @@ struct Profiler {
   double ms[NPASS] = {0};
 };
 
+// Line passes the autotuner chooses an implementation for.
+enum { LP_PSI_Y = 0, LP_PSI_Z = 1, LP_H_Y = 2, LP_H_Z = 3, LP_COUNT = 4 };
+
 struct wdm_ctx {
   wdm_desc d{};
-  int nxh = 0;
+  int nxh = 0;           // half-spectrum columns (nx/2 + 1)
+  int hpitch = 0;        // H row pitch: nxh rounded up to even, so rows are 16-byte
+                         // aligned and H has a tensor-map view for the TMA line passes
   long long ncell = 0;   // cells per batch item
-  long long nhalf = 0;   // half-spectrum entries per batch item
+  long long nhalf = 0;   // H entries per batch item (hpitch * ny * nz, the batch stride)
   cudaStream_t st = nullptr;
   const KernelSet *kx = nullptr, *ky = nullptr, *kz = nullptr;
   double dx = 0, dy = 0, dz = 0, x0 = 0, y0 = 0, z0 = 0;
@@ -124,6 +134,9 @@ struct wdm_ctx {
   int have_psi = 0;
   int phi_valid = 0;
   int64_t launch_count = 0;
+  // autotuned implementation of each line pass (LP_*) and the candidate timings
+  int line_impl[4] = {LINE_IMPL_TMA, LINE_IMPL_TMA, LINE_IMPL_TMA, LINE_IMPL_TMA};
+  double line_ms[4][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
   // adjoint buffers (allocated on first use)
   float2* lam = nullptr;            // adjoint state [batch][ncell]
   float2* Hmu = nullptr;            // half spectrum of mu
@@ -165,13 +178,22 @@ static cudaError_t prof_flush(wdm_ctx* c) {
 }
 
 // Run one pass launch: counted always, bracketed by events when profiling.
+// A launcher outside the KernelSet (the auxiliary kernels) counts as one.
+template <class F>
+static cudaError_t counted(wdm_ctx* c, F launch) {
+  const long long l0 = tl_kernel_launches;
+  const cudaError_t e = launch();
+  const long long n = tl_kernel_launches - l0;
+  c->launch_count += n > 0 ? n : 1;
+  return e;
+}
+
 template <class F>
 static cudaError_t run_pass(wdm_ctx* c, int pass, F launch) {
-  c->launch_count += 1;
-  if (!c->prof.on) return launch();
+  if (!c->prof.on) return counted(c, launch);
   cudaEvent_t a = prof_event(c), b = prof_event(c);
   cudaEventRecord(a, c->st);
-  cudaError_t e = launch();
+  cudaError_t e = counted(c, launch);
   cudaEventRecord(b, c->st);
   c->prof.pending.push_back({pass, a, b});
   if (c->prof.pending.size() > 4096) {
@@ -184,7 +206,7 @@ static cudaError_t run_pass(wdm_ctx* c, int pass, F launch) {
 // Algorithmic bytes of one launch of a pass: every operand read once and
 // written once (complex64 8 B, float 4 B), all batch items.
 static double pass_bytes(const wdm_ctx* c, int p) {
-  const double B = c->d.batch, nc = (double)c->ncell * B, nh = (double)c->nhalf * B;
+  const double B = c->d.batch, nc = (double)c->ncell * B, nh = (double)c->nxh * c->d.ny * c->d.nz * B;
   switch (p) {
     case P_KICK_FWD:
     case P_KICK: return 16.0 * nc + 8.0 * nh + (c->V ? 4.0 * nc : 0.0);
@@ -339,31 +361,35 @@ static RowGeom rows_psi(const wdm_ctx* c) {
   return r;
 }
 
-static LineGeom lines_y(const wdm_ctx* c, int xext, long long bstride) {
+// Lines along y (or z) of an array [batch][nz][ny][pitch] whose first xext
+// entries of a row are data.
+static LineGeom lines_y(const wdm_ctx* c, int xext, long long pitch, long long bstride) {
   LineGeom g;
   g.nlines = xext * c->d.nz;
   g.nxa = xext;
-  g.outer = (long long)c->d.ny * xext;
-  g.pstride = xext;
+  g.outer = (long long)c->d.ny * pitch;
+  g.pstride = pitch;
   g.bstride = bstride;
   g.axis = 1;
   g.rows = c->d.nz;
-  g.pitch = xext;
+  g.pitch = pitch;
   g.err = c->flag + 1;
+  g.impl = c->line_impl[xext == c->nxh ? LP_H_Y : LP_PSI_Y];
   return g;
 }
 
-static LineGeom lines_z(const wdm_ctx* c, int xext, long long bstride) {
+static LineGeom lines_z(const wdm_ctx* c, int xext, long long pitch, long long bstride) {
   LineGeom g;
   g.nlines = xext * c->d.ny;
   g.nxa = xext;
-  g.outer = xext;
-  g.pstride = (long long)c->d.ny * xext;
+  g.outer = pitch;
+  g.pstride = (long long)c->d.ny * pitch;
   g.bstride = bstride;
   g.axis = 2;
   g.rows = c->d.ny;
-  g.pitch = xext;
+  g.pitch = pitch;
   g.err = c->flag + 1;
+  g.impl = c->line_impl[xext == c->nxh ? LP_H_Z : LP_PSI_Z];
   return g;
 }
 
@@ -393,7 +419,7 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.nonfinite = c->flag;
   ra.shift = c->shift;
   cudaError_t e = run_pass(c, write_psi ? P_X_INV_RHO : P_DENSITY, [&] {
-    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, ra, B, c->st);
+    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
   if (c->nparts > 0) {
@@ -402,7 +428,7 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
     });
     if (e != cudaSuccess) return cuda_fail(c, e, "cic clear");
   }
-  if ((e = run_pass(c, P_H_Y_FWD, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st); })) !=
+  if ((e = run_pass(c, P_H_Y_FWD, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y fwd");
   PoissonOp po;
@@ -410,12 +436,11 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   po.ky2 = c->ky2;
   po.kz2 = c->kz2;
   po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
-  po.nxa = c->nxh;
   if ((e = run_pass(c, P_H_Z_POISSON,
-                    [&] { return c->kz->lfft_poisson(c->H, lines_z(c, c->nxh, c->nhalf), c->twz, po, B, c->st); })) !=
+                    [&] { return c->kz->lfft_poisson(c->H, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H z poisson");
-  if ((e = run_pass(c, P_H_Y_INV, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->nhalf), c->twy, true, B, c->st); })) !=
+  if ((e = run_pass(c, P_H_Y_INV, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y inv");
   c->phi_valid = 1;
@@ -459,7 +484,7 @@ static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd, const flo
   KickArgs a = kick_args(c, dt, sched_row);
   const float2* in = psi_in ? psi_in : c->psi;
   cudaError_t e = run_pass(c, fwd ? P_KICK_FWD : P_KICK, [&] {
-    return c->kx->x_kick(in, c->psi, c->H, rows_psi(c), c->nxh, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
+    return c->kx->x_kick(in, c->psi, c->H, rows_psi(c), c->hpitch, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_kick");
   return WDM_OK;
@@ -485,20 +510,19 @@ static wdm_status drift_yz(wdm_ctx* c, double dt, float sign = 1.f, float2* data
   const double scale = 1.0 / ((double)c->d.nx * c->d.ny * c->d.nz);
   op.scale = (float)scale;
   op.scale_lo = (float)(scale - (double)op.scale);
-  op.nxa = c->d.nx;
   op.precise = precise;
   op.tab_bstride = 0;
   cudaError_t e;
   if ((e = run_pass(c, P_PSI_Y_FWD,
-                    [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->ncell), c->twy, false, B, c->st); })) !=
+                    [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->d.nx, c->ncell), c->twy, false, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "psi y fwd");
   if ((e = run_pass(c, P_PSI_Z_DRIFT,
-                    [&] { return c->kz->lfft_drift(psi, lines_z(c, c->d.nx, c->ncell), c->twz, op, B, c->st); })) !=
+                    [&] { return c->kz->lfft_drift(psi, lines_z(c, c->d.nx, c->d.nx, c->ncell), c->twz, op, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "psi z drift");
   if ((e = run_pass(c, P_PSI_Y_INV,
-                    [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->ncell), c->twy, true, B, c->st); })) !=
+                    [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->d.nx, c->ncell), c->twy, true, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "psi y inv");
   return WDM_OK;
@@ -592,6 +616,99 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   return WDM_OK;
 }
 
+// --------------------------------------------------------------------------
+// Line-pass autotuner
+// --------------------------------------------------------------------------
+// Each line pass (psi and H, along y and z) has two implementations: the
+// TMA-fed persistent pass and the register-tile pass.  Which is faster
+// depends on the axis length, the width of the rows (the odd nx/2 + 1 of H
+// leaves a mostly empty last 16-line tile) and the batch, so a new context
+// times both on its own buffers (zeroed; the fused z passes with the Poisson
+// operator) and keeps the faster, preferring TMA within 3%.  Choices are kept
+// per (device, nx, ny, nz, batch); WDM_LINE_IMPL=tma|tile forces one.
+using TuneKey = std::tuple<int, int, int, int, int>;
+struct TuneVal {
+  int impl[LP_COUNT];
+  double ms[LP_COUNT][2];
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneVal> g_tune_cache;
+
+static wdm_status tune_line_passes(wdm_ctx* c) {
+  if (const char* env = std::getenv("WDM_LINE_IMPL")) {
+    if (!std::strcmp(env, "tma") || !std::strcmp(env, "tile")) {
+      const int v = std::strcmp(env, "tma") ? LINE_IMPL_TILE : LINE_IMPL_TMA;
+      for (int k = 0; k < LP_COUNT; ++k) c->line_impl[k] = v;
+      return WDM_OK;
+    }
+  }
+  int dev = 0;
+  WDM_CU(c, cudaGetDevice(&dev));
+  const TuneKey key{dev, c->d.nx, c->d.ny, c->d.nz, c->d.batch};
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto hit = g_tune_cache.find(key);
+  if (hit != g_tune_cache.end()) {
+    std::memcpy(c->line_impl, hit->second.impl, sizeof(c->line_impl));
+    std::memcpy(c->line_ms, hit->second.ms, sizeof(c->line_ms));
+    return WDM_OK;
+  }
+  const int B = c->d.batch;
+  WDM_CU(c, cudaMemsetAsync(c->psi, 0, sizeof(float2) * c->ncell * B, c->st));
+  WDM_CU(c, cudaMemsetAsync(c->H, 0, sizeof(float2) * c->nhalf * B, c->st));
+  PoissonOp po;
+  po.kx2 = c->kx2;
+  po.ky2 = c->ky2;
+  po.kz2 = c->kz2;
+  po.coef = 1.f;
+  auto run = [&](int k) -> cudaError_t {
+    switch (k) {
+      case LP_PSI_Y: return c->ky->lfft(c->psi, lines_y(c, c->d.nx, c->d.nx, c->ncell), c->twy, false, B, c->st);
+      case LP_PSI_Z: return c->kz->lfft_poisson(c->psi, lines_z(c, c->d.nx, c->d.nx, c->ncell), c->twz, po, B, c->st);
+      case LP_H_Y: return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st);
+      default: return c->kz->lfft_poisson(c->H, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st);
+    }
+  };
+  cudaEvent_t e0, e1;
+  WDM_CU(c, cudaEventCreate(&e0));
+  WDM_CU(c, cudaEventCreate(&e1));
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < LP_COUNT && e == cudaSuccess; ++k) {
+    for (int impl = LINE_IMPL_TMA; impl <= LINE_IMPL_TILE && e == cudaSuccess; ++impl) {
+      c->line_impl[k] = impl;
+      double best = 1e30;
+      for (int r = 0; r < 4 && e == cudaSuccess; ++r) {  // the first run is a warm-up
+        if ((e = cudaEventRecord(e0, c->st)) != cudaSuccess || (e = run(k)) != cudaSuccess ||
+            (e = cudaEventRecord(e1, c->st)) != cudaSuccess || (e = cudaEventSynchronize(e1)) != cudaSuccess)
+          break;
+        float ms = 0.f;
+        if ((e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) break;
+        if (r > 0 && ms < best) best = ms;
+      }
+      c->line_ms[k][impl] = best;
+    }
+    c->line_impl[k] = c->line_ms[k][LINE_IMPL_TILE] < 0.97 * c->line_ms[k][LINE_IMPL_TMA] ? LINE_IMPL_TILE
+                                                                                            : LINE_IMPL_TMA;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_fail(c, e, "line-pass autotuner");
+  TuneVal v;
+  std::memcpy(v.impl, c->line_impl, sizeof(v.impl));
+  std::memcpy(v.ms, c->line_ms, sizeof(v.ms));
+  g_tune_cache[key] = v;
+  return WDM_OK;
+}
+
+wdm_status wdm_get_line_schedule(const wdm_ctx* c, int32_t* impl, double* ms) {
+  if (!c || !impl || !ms) return fail(nullptr, WDM_ERR_INVALID, "wdm_get_line_schedule: null argument");
+  for (int k = 0; k < LP_COUNT; ++k) {
+    impl[k] = c->line_impl[k];
+    ms[2 * k] = c->line_ms[k][0];
+    ms[2 * k + 1] = c->line_ms[k][1];
+  }
+  return WDM_OK;
+}
+
 wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   if (!d || !out) return fail(nullptr, WDM_ERR_INVALID, "wdm_create: null argument");
   *out = nullptr;
@@ -613,7 +730,8 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   c->d = *d;
   c->nxh = d->nx / 2 + 1;
   c->ncell = ncell;
-  c->nhalf = (long long)c->nxh * d->ny * d->nz;
+  c->hpitch = c->nxh + (c->nxh & 1);
+  c->nhalf = (long long)c->hpitch * d->ny * d->nz;
   c->kx = kernels_for(d->nx);
   c->ky = kernels_for(d->ny);
   c->kz = kernels_for(d->nz);
@@ -660,6 +778,7 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
     cuda_fail(c, e, "memset shift");
     return bail(WDM_ERR_CUDA);
   }
+  if ((s = tune_line_passes(c)) != WDM_OK) return bail(s);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) {
     cuda_fail(c, e, "sync");
     return bail(WDM_ERR_CUDA);
@@ -696,7 +815,7 @@ static wdm_status phi_real(wdm_ctx* c) {
   WDM_TRY(ensure_scratch(c));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, 0.0));
   cudaError_t e = run_pass(c, P_PHI_OUT, [&] {
-    return c->kx->x_c2r(c->H, c->scratch_f, rows_psi(c), c->nxh, c->nhalf, c->twx, c->d.batch, c->st);
+    return c->kx->x_c2r(c->H, c->scratch_f, rows_psi(c), c->hpitch, c->nhalf, c->twx, c->d.batch, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_c2r");
   return WDM_OK;
@@ -861,22 +980,21 @@ wdm_status wdm_poisson(wdm_ctx* c, const float* rho, float* phi, int32_t where) 
   cudaError_t e;
   if ((e = launch_mean_shift(in, false, c->ncell, B, c->sums, c->shift_in, 0.0, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "mean");
-  if ((e = c->kx->x_r2c(in, c->scratch_h, rows_psi(c), c->nxh, c->nhalf, c->twx, c->shift_in, B, c->st)) != cudaSuccess)
+  if ((e = c->kx->x_r2c(in, c->scratch_h, rows_psi(c), c->hpitch, c->nhalf, c->twx, c->shift_in, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "x r2c");
-  if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess)
+  if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "y fwd");
   PoissonOp po;
   po.kx2 = c->kx2;
   po.ky2 = c->ky2;
   po.kz2 = c->kz2;
   po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
-  po.nxa = c->nxh;
-  if ((e = c->kz->lfft_poisson(c->scratch_h, lines_z(c, c->nxh, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess)
+  if ((e = c->kz->lfft_poisson(c->scratch_h, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "z poisson");
-  if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
+  if ((e = c->ky->lfft(c->scratch_h, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "y inv");
   float* dst = where == WDM_HOST ? c->scratch_f : phi;
-  if ((e = c->kx->x_c2r(c->scratch_h, dst, rows_psi(c), c->nxh, c->nhalf, c->twx, B, c->st)) != cudaSuccess)
+  if ((e = c->kx->x_c2r(c->scratch_h, dst, rows_psi(c), c->hpitch, c->nhalf, c->twx, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "x c2r");
   if (where == WDM_HOST) return copy_out(c, phi, c->scratch_f, bytes, WDM_HOST);
   WDM_CU(c, cudaStreamSynchronize(c->st));
@@ -892,9 +1010,9 @@ wdm_status wdm_fft3d(wdm_ctx* c, void* data, int32_t dir) {
   float2* p = (float2*)data;
   cudaError_t e;
   if ((e = c->kx->xfft(p, rows_psi(c), c->twx, inv, 1.0f, B, c->st)) != cudaSuccess) return cuda_fail(c, e, "x");
-  if ((e = c->ky->lfft(p, lines_y(c, c->d.nx, c->ncell), c->twy, inv, B, c->st)) != cudaSuccess)
+  if ((e = c->ky->lfft(p, lines_y(c, c->d.nx, c->d.nx, c->ncell), c->twy, inv, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "y");
-  if ((e = c->kz->lfft(p, lines_z(c, c->d.nx, c->ncell), c->twz, inv, B, c->st)) != cudaSuccess)
+  if ((e = c->kz->lfft(p, lines_z(c, c->d.nx, c->d.nx, c->ncell), c->twz, inv, B, c->st)) != cudaSuccess)
     return cuda_fail(c, e, "z");
   WDM_CU(c, cudaStreamSynchronize(c->st));
   return WDM_OK;
@@ -1173,7 +1291,6 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   po.ky2 = c->ky2;
   po.kz2 = c->kz2;
   po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
-  po.nxa = c->nxh;
   for (int seg = last_seg; seg >= 0; --seg) {
     const int j0 = seg * ck, j1 = std::min(j0 + ck, nsteps);
     // recompute s_{j0+1..j1} of this segment into the slots, out of place
@@ -1186,17 +1303,18 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
       KickArgs ka = kick_args(c, dtk, b);
       j.pre = st_psi(seg, b);
       const float2* Hb = st_H(seg, b);
-      if ((e = c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->nxh, c->nhalf, c->twx, ka, j, B, c->st)) !=
+      const long long l0 = tl_kernel_launches;
+      if ((e = c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, ka, j, B, c->st)) !=
           cudaSuccess)
         return cuda_fail(c, e, "adjoint kick");
-      if ((e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess ||
-          (e = c->kz->lfft_poisson(c->Hmu, lines_z(c, c->nxh, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess ||
-          (e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
+      if ((e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess ||
+          (e = c->kz->lfft_poisson(c->Hmu, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess ||
+          (e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
         return cuda_fail(c, e, "adjoint Poisson");
-      if ((e = c->kx->adj_apply(c->lam, c->Hmu, rows_psi(c), c->nxh, c->nhalf, c->twx, j, b > 0, B, c->st)) !=
+      if ((e = c->kx->adj_apply(c->lam, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, j, b > 0, B, c->st)) !=
           cudaSuccess)
         return cuda_fail(c, e, "adjoint apply");
-      c->launch_count += 5;
+      c->launch_count += tl_kernel_launches - l0;
       if (b > 0) WDM_TRY(drift_yz(c, dt, -1.f, c->lam));
     }
   }
@@ -1282,7 +1400,9 @@ wdm_status wdm_group_destroy(wdm_group* g) {
 
 int64_t wdm_group_launch_count(const wdm_group* g) { return g ? g->launches : 0; }
 
-wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode) {
+// Capture (first time) and launch the graph of nsteps steps on the group's
+// stream without waiting for it.
+static wdm_status group_enqueue(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode) {
   if (!g || !dts || nsteps < 0) return group_fail(WDM_ERR_INVALID, "wdm_group_step: bad arguments");
   if (nsteps == 0) return WDM_OK;
   const size_t n = g->m.size();
@@ -1335,16 +1455,29 @@ wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32
     hit = &g->cache.back();
   }
   cudaError_t e = cudaGraphLaunch(hit->exec, g->st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(g->st);
   if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
   g->launches += hit->launches;
-  for (size_t i = 0; i < n; ++i) {
-    g->m[i]->launch_count += hit->launches / (int64_t)n;
+  for (size_t i = 0; i < n; ++i) g->m[i]->launch_count += hit->launches / (int64_t)n;
+  return WDM_OK;
+}
+
+wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode) {
+  WDM_TRY(group_enqueue(g, nsteps, dts, mode));
+  if (nsteps == 0) return WDM_OK;
+  cudaError_t e = cudaStreamSynchronize(g->st);
+  if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  for (size_t i = 0; i < g->m.size(); ++i) {
     wdm_status s = sync_and_check(g->m[i]);
     if (s != WDM_OK) return group_fail(s, "wdm_group_step: member " + std::to_string(i) + ": " + g->m[i]->err);
   }
   return WDM_OK;
 }
+
+wdm_status wdm_group_step_async(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode) {
+  return group_enqueue(g, nsteps, dts, mode);
+}
+
+void* wdm_group_stream(const wdm_group* g) { return g ? (void*)g->st : nullptr; }
 
 wdm_status wdm_step_graph(wdm_ctx* c, int32_t nsteps, double dt, int32_t mode) {
   if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
