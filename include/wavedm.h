@@ -191,12 +191,14 @@ wdm_status wdm_set_profiling(wdm_ctx* ctx, int32_t on);
 /* for pass p < WDM_NPASS: launches, summed milliseconds and algorithmic bytes
  * (one read + one write of every operand) of one launch, since profiling on */
 wdm_status wdm_get_profile(wdm_ctx* ctx, int64_t* launches, double* ms, double* bytes_per_launch);
-/* Line-pass schedule chosen by the autotuner when the context was created,
- * for the passes psi-y, psi-z, H-y, H-z in that order: impl[k] = 0 for the
- * TMA-fed persistent pass, 1 for the register-tile pass; ms[2k], ms[2k+1] the
- * best timed milliseconds of the two (-1: not timed, e.g. forced through the
- * environment variable WDM_LINE_IMPL=tma|tile). */
-wdm_status wdm_get_line_schedule(const wdm_ctx* ctx, int32_t impl[4], double ms[8]);
+/* Pass schedule chosen by the autotuner when the context was created, for the
+ * passes psi-y, psi-z, H-y, H-z (line passes: impl 0 = TMA-fed persistent
+ * pass, 1 = register-tile pass) and the kick and density x passes (impl 0 =
+ * rows staged by bulk copies, 1 = rows loaded directly), in that order;
+ * ms[2k], ms[2k+1] the best timed milliseconds of implementations 0 and 1.
+ * The environment variables WDM_LINE_IMPL=tma|tile and
+ * WDM_X_IMPL=staged|direct override the choice. */
+wdm_status wdm_get_line_schedule(const wdm_ctx* ctx, int32_t impl[6], double ms[12]);
 /* number of passes and the name of pass p */
 int32_t wdm_num_passes(void);
 const char* wdm_pass_name(int32_t p);

@@ -279,35 +279,49 @@ def test_bounded_wait_runs_out_and_device_stays_usable(wdm, torch_cuda):
     assert spe.rel_l2(got, ref) < 2e-6
 
 
-@pytest.mark.parametrize("n", [(32, 24, 16), (48, 64, 96), (24, 16, 384)])
-def test_line_pass_implementations_agree(wdm, n, monkeypatch):
-    """The TMA-fed and the register-tile line passes do the same arithmetic, so a
-    run forced onto either one gives the same psi; the autotuner only picks speed."""
+PASS_CASES = [((32, 24, 16), 1), ((48, 64, 96), 1), ((24, 16, 384), 1), ((64, 16, 8), 2), ((384, 8, 8), 1)]
+
+
+@pytest.mark.parametrize("n,batch", PASS_CASES, ids=[f"{'x'.join(map(str, n))}-b{b}" for n, b in PASS_CASES])
+def test_pass_implementations_agree(wdm, n, batch, monkeypatch):
+    """The TMA-fed / register-tile line passes and the staged / direct x passes
+    do the same arithmetic, so runs forced onto either set give the same psi
+    (with tide, Kerr term, absorbing mask and CIC baryons all on); the
+    autotuner only picks speed."""
     nx, ny, nz = n
     L = (4.0, 3.0, 5.0)
     g = spe.Grid(n, L)
     X, Y, Z = g.coords()
     rng = np.random.default_rng(3)
-    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2)) * np.exp(1j * rng.uniform(0, 1, (nz, ny, nx)))).astype(np.complex64)
+    psi0 = np.stack([(np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (1 + b)) * np.exp(1j * rng.uniform(0, 1, (nz, ny, nx))))
+                     for b in range(batch)]).astype(np.complex64).reshape((batch, nz, ny, nx) if batch > 1 else (nz, ny, nx))
+    pos = rng.uniform(-1.0, 1.0, (50, 3))
+    T = np.array([[0.3, -0.1, -0.2, 0.05, 0.0, 0.02]] * 4)
     out = {}
-    for impl in ("tma", "tile"):
-        monkeypatch.setenv("WDM_LINE_IMPL", impl)
-        with wdm.SPEContext(n, L, poisson_coeff=2.0) as ctx:
+    for line_impl, x_impl in (("tma", "staged"), ("tile", "direct")):
+        monkeypatch.setenv("WDM_LINE_IMPL", line_impl)
+        monkeypatch.setenv("WDM_X_IMPL", x_impl)
+        with wdm.SPEContext(n, L, poisson_coeff=2.0, kerr=0.3, absorb_alpha=0.5, batch=batch) as ctx:
             sched = ctx.line_schedule()
-            assert all(v["impl"] == impl for v in sched.values())
+            assert [v["impl"] for v in sched.values()] == [line_impl] * 4 + [x_impl] * 2
             ctx.set_psi(psi0)
+            ctx.set_tidal(T)
+            if batch == 1:
+                ctx.set_particles(pos, 0.01)
             ctx.step(3, 0.01)
-            out[impl] = ctx.get_psi()
+            out[line_impl] = ctx.get_psi()
     assert np.array_equal(out["tma"], out["tile"])
 
 
 def test_autotuner_reports_a_schedule(wdm, monkeypatch):
     monkeypatch.delenv("WDM_LINE_IMPL", raising=False)
+    monkeypatch.delenv("WDM_X_IMPL", raising=False)
     with wdm.SPEContext((64, 64, 64), (1.0, 1.0, 1.0)) as ctx:
         sched = ctx.line_schedule()
-    assert set(sched) == {"psi_y", "psi_z", "h_y", "h_z"}
+    assert list(sched) == ["psi_y", "psi_z", "h_y", "h_z", "x_kick", "x_rho"]
     for v in sched.values():
-        assert v["impl"] in ("tma", "tile")
-        assert 0 < v["ms_tma"] < 1e3 and 0 < v["ms_tile"] < 1e3
-        faster = "tile" if v["ms_tile"] < 0.97 * v["ms_tma"] else "tma"
+        names = list(v["ms"])
+        assert v["impl"] in names
+        assert all(0 < t < 1e3 for t in v["ms"].values())
+        faster = names[1] if v["ms"][names[1]] < 0.97 * v["ms"][names[0]] else names[0]
         assert v["impl"] == faster

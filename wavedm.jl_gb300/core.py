@@ -229,17 +229,19 @@ class SPEContext:
         return {self.lib.wdm_pass_name(p).decode(): dict(launches=int(la[p]), ms=float(ms[p]),
                                                           bytes_per_launch=float(by[p])) for p in range(n)}
 
-    LINE_PASSES = ("psi_y", "psi_z", "h_y", "h_z")
-    LINE_IMPLS = ("tma", "tile")
+    # tuned passes and the names of their two implementations
+    SCHEDULE = (("psi_y", ("tma", "tile")), ("psi_z", ("tma", "tile")), ("h_y", ("tma", "tile")),
+                ("h_z", ("tma", "tile")), ("x_kick", ("staged", "direct")), ("x_rho", ("staged", "direct")))
 
     def line_schedule(self):
-        """{line pass: dict(impl, ms_tma, ms_tile)} as chosen by the autotuner at creation."""
-        impl = np.zeros(4, np.int32)
-        ms = np.zeros(8, np.float64)
+        """{pass: dict(impl, ms={impl name: best ms})} as chosen by the autotuner at creation."""
+        n = len(self.SCHEDULE)
+        impl = np.zeros(n, np.int32)
+        ms = np.zeros(2 * n, np.float64)
         self._check(self.lib.wdm_get_line_schedule(self.handle, C.c_void_p(impl.ctypes.data),
                                                    C.c_void_p(ms.ctypes.data)))
-        return {name: dict(impl=self.LINE_IMPLS[int(impl[k])], ms_tma=float(ms[2 * k]), ms_tile=float(ms[2 * k + 1]))
-                for k, name in enumerate(self.LINE_PASSES)}
+        return {name: dict(impl=names[int(impl[k])], ms={names[0]: float(ms[2 * k]), names[1]: float(ms[2 * k + 1])})
+                for k, (name, names) in enumerate(self.SCHEDULE)}
 
     @property
     def launch_count(self):

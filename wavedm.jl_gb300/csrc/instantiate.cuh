@@ -153,32 +153,68 @@ struct Launch {
     }
     return cudaGetLastError();
   }
+  // Staged x passes: the layout conditions of their bulk copies.  Rows of
+  // 16-byte multiples at 16-byte aligned addresses (the half spectrum with the
+  // even pitch nx/2 + 2), and units of GROUPS row pairs inside one batch item.
+  using XS = XStage<N>;
+  static bool x_staged_ok(const RowGeom& rg, long long hpitch, const void* p0, const void* p1, const void* p2) {
+    if (rg.impl != X_IMPL_STAGED || hpitch != XS::HP || rg.pitch != N) return false;
+    if ((rg.nrows / 2) % XCfg<N>::GROUPS != 0 || rg.nrows % 2 != 0) return false;
+    for (const void* p : {p0, p1, p2})
+      if (reinterpret_cast<uintptr_t>(p) % 16) return false;
+    return true;
+  }
+  template <auto K>
+  static dim3 grid_xs(const RowGeom& rg, int batch, XWork* w) {
+    w->pairs_per_item = rg.nrows / 2;
+    w->batch = batch;
+    const long long units = (long long)w->pairs_per_item * batch / XCfg<N>::GROUPS;
+    const long long ctas = (units + XCfg<N>::WARPS - 1) / XCfg<N>::WARPS;
+    const long long cap = (long long)resident_ctas<K>(XNT, XS::SMEM) * sm_count();
+    return dim3((unsigned)(ctas < cap ? ctas : cap));
+  }
   static cudaError_t x_inv_rho(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
                                const float4* tw, const RhoArgs& a, int batch, cudaStream_t st) {
     cudaError_t e;
     XWork w;
+    if (x_staged_ok(rg, hpitch, psi, H, a.rho_b) && (!a.rho_b || (a.rb_bstride * 4) % 16 == 0)) {
+      constexpr auto K = k_xs_inv_rho<N>;
+      if ((e = prep_once<K>(XS::SMEM)) != cudaSuccess) return e;
+      const dim3 gr = grid_xs<K>(rg, batch, &w);
+      K<<<gr, XNT, XS::SMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
+      ++tl_kernel_launches;
+      return cudaGetLastError();
+    }
     const dim3 gr = grid_x(rg, batch, &w);
     if ((e = prep_once<k_xw_inv_rho<N>>(XSMEM)) != cudaSuccess) return e;
     k_xw_inv_rho<N><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
     ++tl_kernel_launches;
     return cudaGetLastError();
   }
+  template <bool FWD>
+  static cudaError_t x_kick_t(const float2* psi_in, float2* psi, const float2* H, const RowGeom& rg, long long hpitch,
+                              long long hbstride, const float4* tw, const KickArgs& a, int batch, cudaStream_t st) {
+    cudaError_t e;
+    XWork w;
+    if (x_staged_ok(rg, hpitch, psi_in, psi, H)) {
+      constexpr auto K = k_xs_kick<N, FWD>;
+      if ((e = prep_once<K>(XS::SMEM)) != cudaSuccess) return e;
+      const dim3 gr = grid_xs<K>(rg, batch, &w);
+      K<<<gr, XNT, XS::SMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
+      ++tl_kernel_launches;
+      return cudaGetLastError();
+    }
+    const dim3 gr = grid_x(rg, batch, &w);
+    if ((e = prep_once<k_xw_kick<N, FWD>>(XSMEM)) != cudaSuccess) return e;
+    k_xw_kick<N, FWD><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
+    ++tl_kernel_launches;
+    return cudaGetLastError();
+  }
   static cudaError_t x_kick(const float2* psi_in, float2* psi, const float2* H, const RowGeom& rg, long long hpitch,
                             long long hbstride, const float4* tw, const KickArgs& a, bool fwd, int batch,
                             cudaStream_t st) {
-    cudaError_t e;
-    XWork w;
-    const dim3 gr = grid_x(rg, batch, &w);
-    if (fwd) {
-      if ((e = prep_once<k_xw_kick<N, true>>(XSMEM)) != cudaSuccess) return e;
-      k_xw_kick<N, true><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
-      ++tl_kernel_launches;
-    } else {
-      if ((e = prep_once<k_xw_kick<N, false>>(XSMEM)) != cudaSuccess) return e;
-      k_xw_kick<N, false><<<gr, XNT, XSMEM, st>>>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, w);
-      ++tl_kernel_launches;
-    }
-    return cudaGetLastError();
+    return fwd ? x_kick_t<true>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, batch, st)
+               : x_kick_t<false>(psi_in, psi, H, rg, hpitch, hbstride, tw, a, batch, st);
   }
   static cudaError_t x_c2r(const float2* H, float* out, const RowGeom& rg, long long hpitch, long long hbstride,
                            const float4* tw, int batch, cudaStream_t st) {

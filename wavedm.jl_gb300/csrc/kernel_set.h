@@ -3,7 +3,7 @@
 // build parallelises) and exposes wdm_ks_<N>().
 #pragma once
 #include <cuda_runtime.h>
-#include "xpass_warp.cuh"
+#include "xpass_staged.cuh"
 
 namespace wdm {
 

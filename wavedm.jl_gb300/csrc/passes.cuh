@@ -69,7 +69,13 @@ struct RowGeom {
   int ny;             // rows per z plane
   long long pitch;    // element stride between rows
   long long bstride;  // element stride between batch items
+  int impl = 0;       // X_IMPL_STAGED or X_IMPL_DIRECT for the kick and density passes
 };
+
+// Implementations of the kick and density x passes: rows staged in shared
+// memory by bulk copies one unit ahead (where the layout allows), or loaded
+// straight into registers.
+enum { X_IMPL_STAGED = 0, X_IMPL_DIRECT = 1 };
 
 __device__ __forceinline__ long long line_base(const LineGeom& g, int line) {
   return (long long)(line / g.nxa) * g.outer + (line % g.nxa);
@@ -443,6 +449,7 @@ struct RhoArgs {
   long long rb_bstride;
   int write_psi;     // 0: density only (psi is already in real space, left untouched)
   int* nonfinite;    // set to 1 when any density value is NaN/Inf (null: unchecked)
+  int* err = nullptr;  // error word of abandoned waits of the staged pass (may be null)
   // Per-batch-item constant subtracted from rho before the transform (an
   // estimate of its mean).  Only the k = 0 mode changes, which the Poisson
   // solve drops, so any value is exact; a value near the mean keeps the FP32
@@ -463,6 +470,7 @@ struct KickArgs {
   const float* V;        // static potential [nz][ny][nx] or null
   long long v_bstride;
   int precise;           // reduce the phase modulo 2 pi in float-float before sincos
+  int* err = nullptr;    // error word of abandoned waits of the staged pass (may be null)
 };
 
 // psi * exp(-i dt pot).

@@ -94,7 +94,9 @@ struct Profiler {
 };
 
 // Line passes the autotuner chooses an implementation for.
-enum { LP_PSI_Y = 0, LP_PSI_Z = 1, LP_H_Y = 2, LP_H_Z = 3, LP_COUNT = 4 };
+// (the x passes' choice is X_IMPL_STAGED / X_IMPL_DIRECT, the line passes' LINE_IMPL_TMA / LINE_IMPL_TILE;
+// 0 is the preferred implementation of each)
+enum { LP_PSI_Y = 0, LP_PSI_Z = 1, LP_H_Y = 2, LP_H_Z = 3, LP_X_KICK = 4, LP_X_RHO = 5, LP_COUNT = 6 };
 
 struct wdm_ctx {
   wdm_desc d{};
@@ -135,8 +137,8 @@ struct wdm_ctx {
   int phi_valid = 0;
   int64_t launch_count = 0;
   // autotuned implementation of each line pass (LP_*) and the candidate timings
-  int line_impl[4] = {LINE_IMPL_TMA, LINE_IMPL_TMA, LINE_IMPL_TMA, LINE_IMPL_TMA};
-  double line_ms[4][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
+  int line_impl[LP_COUNT] = {0, 0, 0, 0, 0, 0};
+  double line_ms[LP_COUNT][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
   // adjoint buffers (allocated on first use)
   float2* lam = nullptr;            // adjoint state [batch][ncell]
   float2* Hmu = nullptr;            // half spectrum of mu
@@ -361,6 +363,13 @@ static RowGeom rows_psi(const wdm_ctx* c) {
   return r;
 }
 
+// The rows of psi for the tuned x pass `kind` (LP_X_KICK or LP_X_RHO).
+static RowGeom rows_psi(const wdm_ctx* c, int kind) {
+  RowGeom r = rows_psi(c);
+  r.impl = c->line_impl[kind];
+  return r;
+}
+
 // Lines along y (or z) of an array [batch][nz][ny][pitch] whose first xext
 // entries of a row are data.
 static LineGeom lines_y(const wdm_ctx* c, int xext, long long pitch, long long bstride) {
@@ -418,8 +427,9 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.write_psi = write_psi;
   ra.nonfinite = c->flag;
   ra.shift = c->shift;
+  ra.err = c->flag + 1;
   cudaError_t e = run_pass(c, write_psi ? P_X_INV_RHO : P_DENSITY, [&] {
-    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
+    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, LP_X_RHO), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
   if (c->nparts > 0) {
@@ -476,6 +486,7 @@ static KickArgs kick_args(const wdm_ctx* c, double dt, int sched_row) {
   a.V = c->V;
   a.v_bstride = c->ncell;
   a.precise = c->d.phase_mode == WDM_PHASE_PRECISE;
+  a.err = c->flag + 1;
   return a;
 }
 
@@ -484,7 +495,7 @@ static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd, const flo
   KickArgs a = kick_args(c, dt, sched_row);
   const float2* in = psi_in ? psi_in : c->psi;
   cudaError_t e = run_pass(c, fwd ? P_KICK_FWD : P_KICK, [&] {
-    return c->kx->x_kick(in, c->psi, c->H, rows_psi(c), c->hpitch, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
+    return c->kx->x_kick(in, c->psi, c->H, rows_psi(c, LP_X_KICK), c->hpitch, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_kick");
   return WDM_OK;
@@ -619,13 +630,16 @@ wdm_status wdm_destroy(wdm_ctx* c) {
 // --------------------------------------------------------------------------
 // Line-pass autotuner
 // --------------------------------------------------------------------------
-// Each line pass (psi and H, along y and z) has two implementations: the
-// TMA-fed persistent pass and the register-tile pass.  Which is faster
-// depends on the axis length, the width of the rows (the odd nx/2 + 1 of H
-// leaves a mostly empty last 16-line tile) and the batch, so a new context
-// times both on its own buffers (zeroed; the fused z passes with the Poisson
-// operator) and keeps the faster, preferring TMA within 3%.  Choices are kept
-// per (device, nx, ny, nz, batch); WDM_LINE_IMPL=tma|tile forces one.
+// Each line pass (psi and H, along y and z) has two implementations, the
+// TMA-fed persistent pass and the register-tile pass, and the kick and
+// density x passes two, rows staged by bulk copies or loaded directly.  Which
+// is faster depends on the axis length, the width of the rows (the odd
+// nx/2 + 1 of H leaves a mostly empty last 16-line tile), the batch and the
+// occupancy the staging slots leave, so a new context times both of every
+// pass on its own buffers (zeroed; the fused z passes with the Poisson
+// operator, the kick with a small time step) and keeps the faster, preferring
+// implementation 0 within 3%.  Choices are kept per (device, nx, ny, nz,
+// batch); WDM_LINE_IMPL=tma|tile and WDM_X_IMPL=staged|direct force them.
 using TuneKey = std::tuple<int, int, int, int, int>;
 struct TuneVal {
   int impl[LP_COUNT];
@@ -634,14 +648,52 @@ struct TuneVal {
 static std::mutex g_tune_mu;
 static std::map<TuneKey, TuneVal> g_tune_cache;
 
-static wdm_status tune_line_passes(wdm_ctx* c) {
+// Implementations forced through the environment (after tuning; not cached).
+static void forced_impls(wdm_ctx* c) {
   if (const char* env = std::getenv("WDM_LINE_IMPL")) {
-    if (!std::strcmp(env, "tma") || !std::strcmp(env, "tile")) {
-      const int v = std::strcmp(env, "tma") ? LINE_IMPL_TILE : LINE_IMPL_TMA;
-      for (int k = 0; k < LP_COUNT; ++k) c->line_impl[k] = v;
-      return WDM_OK;
-    }
+    if (!std::strcmp(env, "tma") || !std::strcmp(env, "tile"))
+      for (int k = LP_PSI_Y; k <= LP_H_Z; ++k) c->line_impl[k] = std::strcmp(env, "tma") ? LINE_IMPL_TILE : LINE_IMPL_TMA;
   }
+  if (const char* env = std::getenv("WDM_X_IMPL")) {
+    if (!std::strcmp(env, "staged") || !std::strcmp(env, "direct"))
+      for (int k = LP_X_KICK; k <= LP_X_RHO; ++k)
+        c->line_impl[k] = std::strcmp(env, "staged") ? X_IMPL_DIRECT : X_IMPL_STAGED;
+  }
+}
+
+static wdm_status tune_passes_timed(wdm_ctx* c);
+
+// WDM_SCHEDULE="a,b,c,d,e,f": the whole schedule (psi-y, psi-z, H-y, H-z as
+// tma|tile; kick, density as staged|direct), no timing (e.g. under a profiler).
+static bool schedule_from_env(wdm_ctx* c) {
+  const char* env = std::getenv("WDM_SCHEDULE");
+  if (!env) return false;
+  static const char* const names[2][2] = {{"tma", "tile"}, {"staged", "direct"}};
+  int impl[LP_COUNT];
+  std::string s(env);
+  size_t pos = 0;
+  for (int k = 0; k < LP_COUNT; ++k) {
+    const size_t end = s.find(',', pos);
+    const std::string tok = s.substr(pos, end == std::string::npos ? std::string::npos : end - pos);
+    const int kind = k < LP_X_KICK ? 0 : 1;
+    if (tok == names[kind][0]) impl[k] = 0;
+    else if (tok == names[kind][1]) impl[k] = 1;
+    else return false;
+    if (end == std::string::npos && k + 1 < LP_COUNT) return false;
+    pos = end + 1;
+  }
+  std::memcpy(c->line_impl, impl, sizeof(impl));
+  return true;
+}
+
+static wdm_status tune_passes(wdm_ctx* c) {
+  if (schedule_from_env(c)) return WDM_OK;
+  WDM_TRY(tune_passes_timed(c));
+  forced_impls(c);
+  return WDM_OK;
+}
+
+static wdm_status tune_passes_timed(wdm_ctx* c) {
   int dev = 0;
   WDM_CU(c, cudaGetDevice(&dev));
   const TuneKey key{dev, c->d.nx, c->d.ny, c->d.nz, c->d.batch};
@@ -660,12 +712,22 @@ static wdm_status tune_line_passes(wdm_ctx* c) {
   po.ky2 = c->ky2;
   po.kz2 = c->kz2;
   po.coef = 1.f;
+  const KickArgs ka = kick_args(c, 1e-3, 0);
+  RhoArgs ra{};
+  ra.write_psi = 1;
+  ra.nonfinite = c->flag;
+  ra.shift = c->shift;
+  ra.err = c->flag + 1;
   auto run = [&](int k) -> cudaError_t {
     switch (k) {
       case LP_PSI_Y: return c->ky->lfft(c->psi, lines_y(c, c->d.nx, c->d.nx, c->ncell), c->twy, false, B, c->st);
       case LP_PSI_Z: return c->kz->lfft_poisson(c->psi, lines_z(c, c->d.nx, c->d.nx, c->ncell), c->twz, po, B, c->st);
       case LP_H_Y: return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st);
-      default: return c->kz->lfft_poisson(c->H, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st);
+      case LP_H_Z: return c->kz->lfft_poisson(c->H, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st);
+      case LP_X_KICK:
+        return c->kx->x_kick(c->psi, c->psi, c->H, rows_psi(c, LP_X_KICK), c->hpitch, c->nhalf, c->twx, ka, true, B,
+                             c->st);
+      default: return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, LP_X_RHO), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
     }
   };
   cudaEvent_t e0, e1;
@@ -673,7 +735,7 @@ static wdm_status tune_line_passes(wdm_ctx* c) {
   WDM_CU(c, cudaEventCreate(&e1));
   cudaError_t e = cudaSuccess;
   for (int k = 0; k < LP_COUNT && e == cudaSuccess; ++k) {
-    for (int impl = LINE_IMPL_TMA; impl <= LINE_IMPL_TILE && e == cudaSuccess; ++impl) {
+    for (int impl = 0; impl <= 1 && e == cudaSuccess; ++impl) {
       c->line_impl[k] = impl;
       double best = 1e30;
       for (int r = 0; r < 4 && e == cudaSuccess; ++r) {  // the first run is a warm-up
@@ -686,8 +748,7 @@ static wdm_status tune_line_passes(wdm_ctx* c) {
       }
       c->line_ms[k][impl] = best;
     }
-    c->line_impl[k] = c->line_ms[k][LINE_IMPL_TILE] < 0.97 * c->line_ms[k][LINE_IMPL_TMA] ? LINE_IMPL_TILE
-                                                                                            : LINE_IMPL_TMA;
+    c->line_impl[k] = c->line_ms[k][1] < 0.97 * c->line_ms[k][0] ? 1 : 0;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -778,7 +839,7 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
     cuda_fail(c, e, "memset shift");
     return bail(WDM_ERR_CUDA);
   }
-  if ((s = tune_line_passes(c)) != WDM_OK) return bail(s);
+  if ((s = tune_passes(c)) != WDM_OK) return bail(s);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) {
     cuda_fail(c, e, "sync");
     return bail(WDM_ERR_CUDA);

@@ -1,0 +1,255 @@
+// x passes with their input rows staged in shared memory by 1-D bulk copies.
+//
+// The direct kernels (xpass_warp.cuh) load each row into registers when they
+// reach it, so a warp waits on global memory three times per row pair (the
+// potential rows, then psi row A, then psi row B) with nothing else to do.
+// Here every warp owns two slots: slot A for the half-spectrum rows (kick) or
+// the baryon density rows (density pass), slot B for the psi rows of a whole
+// unit (the GROUPS row pairs of one warp).  As soon as a slot's rows are in
+// registers the warp's lane 0 issues the bulk copies of the same rows of its
+// next unit into it, so those copies run under the transforms of the current
+// unit.  Each row is one copy into a slot row whose pitch is padded by 16
+// bytes, so that the lane groups of a warp read different banks.  The slots
+// cost occupancy (3 CTAs of 4 warps per SM at N = 384) but leave each thread
+// up to 168 registers.  Every wait is bounded: a warp that gives up records
+// WDM_DEVERR_TMA_WAIT, drains its copies (bounded) and exits.
+#pragma once
+#include "xpass_warp.cuh"
+
+namespace wdm {
+
+template <int N>
+struct XStage {
+  using C = XCfg<N>;
+  static constexpr int G = C::GROUPS;
+  static constexpr int ROWS = 2 * G;    // rows of one warp unit
+  static constexpr int HP = N / 2 + 2;  // H row pitch in global memory: nx/2 + 1 rounded up to even
+  static constexpr int PSI_P = N + 2;   // staged psi row pitch (float2)
+  static constexpr int H_P = HP + 2;    // staged H row pitch (float2)
+  static constexpr int RB_P = N + 4;    // staged density row pitch (float)
+  static constexpr size_t A_BYTES = sizeof(float2) * ROWS * H_P;
+  static constexpr size_t B_BYTES = sizeof(float2) * ROWS * PSI_P;
+  static_assert(sizeof(float) * ROWS * RB_P <= A_BYTES, "density rows fit slot A");
+  static constexpr size_t WARP_BYTES = A_BYTES + B_BYTES;
+  static constexpr size_t BASE = C::SMEM;  // after the twiddle tables and exchange buffers
+  static constexpr size_t SMEM = BASE + C::WARPS * WARP_BYTES + C::WARPS * 2 * sizeof(uint64_t);
+  // resident CTAs per SM the shared memory allows (at most 4), for the register budget
+  static constexpr int MINB_RAW = (int)((228u * 1024u) / (SMEM + 1024u));
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+  static_assert(BASE % 16 == 0 && A_BYTES % 16 == 0 && B_BYTES % 16 == 0, "16-byte aligned slots");
+};
+
+// Copy `nrows` rows of `row_elems` elements (pitch src_pitch) to a slot with
+// row pitch dst_pitch, all completing on `bar` (one lane).
+template <typename E>
+__device__ __forceinline__ void stage_rows(E* dst, int dst_pitch, const E* src, long long src_pitch, int row_elems,
+                                           int nrows, uint64_t* bar) {
+  const unsigned rb = (unsigned)(row_elems * sizeof(E));
+  mbar_expect_tx(bar, rb * (unsigned)nrows);
+  for (int r = 0; r < nrows; ++r) bulk_g2s(dst + r * dst_pitch, src + r * src_pitch, rb, bar);
+}
+
+// Bounded wait, uniform over the warp.
+__device__ __forceinline__ bool xwait(uint64_t* bar, unsigned parity) {
+  return __all_sync(0xffffffffu, mbar_wait_bounded(bar, parity));
+}
+
+// The slot's rows are in registers: order those reads before the next copy.
+__device__ __forceinline__ void xrelease() {
+  fence_proxy_async_smem();
+  __syncwarp();
+}
+
+#define WDM_XSTAGE_PROLOGUE                                                                          \
+  using S = XStage<N>;                                                                               \
+  unsigned char* sraw = reinterpret_cast<unsigned char*>(smem);                                      \
+  unsigned char* wslots = sraw + S::BASE + (size_t)warp * S::WARP_BYTES;                             \
+  float2* slotA = reinterpret_cast<float2*>(wslots);                                                 \
+  float2* slotB = reinterpret_cast<float2*>(wslots + S::A_BYTES);                                    \
+  uint64_t* xbar = reinterpret_cast<uint64_t*>(sraw + S::BASE + (size_t)C::WARPS * S::WARP_BYTES) + 2 * warp; \
+  if (lane == 0) {                                                                                   \
+    mbar_init(&xbar[0], 1);                                                                          \
+    mbar_init(&xbar[1], 1);                                                                          \
+    mbar_fence_init();                                                                               \
+  }                                                                                                  \
+  __syncwarp();                                                                                      \
+  const int ppi = w.pairs_per_item;                                                                  \
+  unsigned pend = 0, ph = 0; /* bit s: slot s has copies in flight / parity of its next phase */
+
+// Wait for slot s (bounded, warp-uniform); false: give up.
+#define WDM_XSTAGE_WAIT(s) \
+  (xwait(&xbar[(s)], (ph >> (s)) & 1u) ? (ph ^= 1u << (s), pend &= ~(1u << (s)), true) : false)
+
+// Give up: record the error, drain this warp's copies (bounded), leave.
+#define WDM_XSTAGE_FAIL(errp)                                                        \
+  do {                                                                               \
+    if (lane == 0 && (errp)) atomicOr((errp), WDM_DEVERR_TMA_WAIT);                  \
+    bool drained = true;                                                             \
+    for (int s_ = 0; s_ < 2; ++s_)                                                   \
+      if (pend & (1u << s_)) drained = xwait(&xbar[s_], (ph >> s_) & 1u) && drained; \
+    if (lane == 0 && (errp) && !drained) atomicOr((errp), WDM_DEVERR_TMA_DRAIN);     \
+    return;                                                                          \
+  } while (0)
+
+// first batch item and row of warp unit u (a unit never straddles two items:
+// the launcher requires GROUPS to divide the row pairs of an item)
+__device__ __forceinline__ void unit_rows(long long u, int groups, int ppi, int* b, int* ra) {
+  const long long pp0 = u * groups;
+  *b = (int)(pp0 / ppi);
+  *ra = 2 * (int)(pp0 - (long long)(*b) * ppi);
+}
+
+// P1 (staged): Phi rows from H, kick, forward x transform (FWD) or not.
+template <int N, bool FWD>
+__global__ void __launch_bounds__(XCfg<N>::NT, XStage<N>::MINB)
+k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGeom rg, long long hpitch,
+          long long hbstride, const float4* __restrict__ twg, KickArgs a, XWork w) {
+  WDM_XPASS_PROLOGUE
+  WDM_XSTAGE_PROLOGUE
+  using Rev = typename Reverse<Rad>::type;
+  auto issue_h = [&](long long u) {
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    stage_rows(slotA, S::H_P, H + b * hbstride + ra * hpitch, hpitch, S::HP, S::ROWS, &xbar[0]);
+  };
+  auto issue_p = [&](long long u) {
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    stage_rows(slotB, S::PSI_P, psi_in + b * rg.bstride + ra * rg.pitch, rg.pitch, N, S::ROWS, &xbar[1]);
+  };
+  long long u = (long long)blockIdx.x * C::WARPS + warp;
+  if (u < nunits) {
+    if (lane == 0) {
+      issue_h(u);
+      issue_p(u);
+    }
+    pend = 3u;
+  }
+  for (; u < nunits; u += wstride) {
+    const long long un = u + wstride;
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    ra += 2 * g;  // this lane group's pair
+    if (!WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
+    float2 v[N / T];
+    load_packed_half<N, T, RadInfo<Rev>::first>(v, slotA + (2 * g) * S::H_P, slotA + (2 * g + 1) * S::H_P, true, t);
+    xrelease();
+    if (un < nunits) {
+      if (lane == 0) issue_h(un);
+      pend |= 1u;
+    }
+    run_wstages<N, T, C::NP, true>(Rev{}, v, buf, twr, t);  // ends with radix R1
+    float phi[2][N / T];
+#pragma unroll
+    for (int q = 0; q < N / T; ++q) {
+      phi[0][q] = v[q].x;
+      phi[1][q] = v[q].y;
+    }
+    float T6[6];
+    kick_tidal<N>(T6, a, b);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      if (half == 0 && !WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
+      const float2* srow = slotB + (2 * g + half) * S::PSI_P;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) v[i * R1 + k] = srow[slot_pos<N, T, R1>(t, i, k)];
+      if (half == 1) {
+        xrelease();
+        if (un < nunits) {
+          if (lane == 0) issue_p(un);
+          pend |= 2u;
+        }
+      }
+      const int r = ra + half;
+      kick_row<N, FWD>(v, phi[half], T6, a, rg, r, b, true, psi + b * rg.bstride + (long long)r * rg.pitch, buf, tw,
+                       t);
+    }
+  }
+}
+
+// P5 (staged): psi x-inverse (+mask), rho = |psi|^2 (+rho_b) - shift, packed R2C -> H.
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, XStage<N>::MINB)
+k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
+             const float4* __restrict__ twg, RhoArgs a, XWork w) {
+  WDM_XPASS_PROLOGUE
+  WDM_XSTAGE_PROLOGUE
+  float* rbslot = reinterpret_cast<float*>(slotA);
+  auto issue_p = [&](long long u) {
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    stage_rows(slotB, S::PSI_P, psi + b * rg.bstride + ra * rg.pitch, rg.pitch, N, S::ROWS, &xbar[1]);
+  };
+  auto issue_r = [&](long long u) {
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    stage_rows(rbslot, S::RB_P, a.rho_b + b * a.rb_bstride + ra * rg.pitch, rg.pitch, N, S::ROWS, &xbar[0]);
+  };
+  const bool with_rb = a.rho_b != nullptr;
+  long long u = (long long)blockIdx.x * C::WARPS + warp;
+  if (u < nunits) {
+    if (lane == 0) {
+      issue_p(u);
+      if (with_rb) issue_r(u);
+    }
+    pend = with_rb ? 3u : 2u;
+  }
+  for (; u < nunits; u += wstride) {
+    const long long un = u + wstride;
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    ra += 2 * g;
+    const float shift = a.shift ? a.shift[b] : 0.f;
+    float rho0[N / T];  // row A density at radix-RS slots
+    float2 z[N / T];    // packed (rho_A, rho_B) at radix-RS slots
+    float2 v[N / T];
+    if (!WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const float2* srow = slotB + (2 * g + half) * S::PSI_P;
+      if (a.write_psi) {
+#pragma unroll
+        for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+          for (int k = 0; k < R1; ++k) v[i * R1 + k] = srow[slot_pos<N, T, R1>(t, i, k)];
+      } else {
+#pragma unroll
+        for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+          for (int k = 0; k < RS; ++k) v[i * RS + k] = srow[slot_pos<N, T, RS>(t, i, k)];
+      }
+      if (half == 1) {
+        xrelease();
+        if (un < nunits) {
+          if (lane == 0) issue_p(un);
+          pend |= 2u;
+        }
+      }
+      if (half == 0 && with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
+      const int r = ra + half;
+      const float* rb = with_rb ? rbslot + (2 * g + half) * S::RB_P : nullptr;
+      inv_rho_row<N>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb, shift, half, rho0, z,
+                     buf, tw, t);
+      if (half == 1 && with_rb) {
+        xrelease();
+        if (un < nunits) {
+          if (lane == 0) issue_r(un);
+          pend |= 1u;
+        }
+      }
+    }
+    reorder<N, T, RS, R1>(z, v);
+    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+    float2* hrow = H + b * hbstride + ra * hpitch;
+    store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, true, t);
+  }
+}
+
+#undef WDM_XSTAGE_FAIL
+#undef WDM_XSTAGE_WAIT
+#undef WDM_XSTAGE_PROLOGUE
+#undef WDM_XPASS_PROLOGUE
+
+}  // namespace wdm

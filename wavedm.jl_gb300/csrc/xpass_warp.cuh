@@ -250,6 +250,60 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
 // ----------------------------------------------------------------------------
 // P1: Phi rows from H (C2R of the packed pair), kick, forward x-FFT (or not)
 // ----------------------------------------------------------------------------
+// One row of the kick pass: v holds psi row r at radix-R1 slots, phi its
+// potential at the same slots; kick, then (FWD) the forward x transform, and
+// store to `row` (when ok).  Shared by the direct and the staged kernels.
+template <int N, bool FWD>
+__device__ __forceinline__ void kick_row(float2* v, const float* phi, const float* T6, const KickArgs& a,
+                                         const RowGeom& rg, int r, int b, bool ok, float2* row, float2* buf,
+                                         const float4* tw, int t) {
+  using C = XCfg<N>;
+  constexpr int T = C::T;
+  using Rad = typename XPlan<N>::Fwd;
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
+  const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
+  const int y = r % rg.ny, z = r / rg.ny;
+  const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * z;
+  // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2)
+  const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
+  const float lin = T6[3] * fy + T6[4] * fz;
+#pragma unroll
+  for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+    for (int k = 0; k < R1; ++k) {
+      const int q = i * R1 + k;
+      const int x = slot_pos<N, T, R1>(t, i, k);
+      float pot = phi[q];
+      if (a.tidal) {
+        const float fx = a.x0 + a.dx * x;
+        pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
+      }
+      if (a.kerr != 0.f) pot += a.kerr * (v[q].x * v[q].x + v[q].y * v[q].y);
+      if (vrow && ok) pot += vrow[x];
+      v[q] = apply_kick(v[q], pot, a);
+    }
+  if constexpr (FWD) {
+    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+    if (ok)
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+  } else {
+    if (ok)
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) row[slot_pos<N, T, R1>(t, i, k)] = v[i * R1 + k];
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, int b) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
+}
+
 template <int N, bool FWD>
 __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGeom rg, long long hpitch,
@@ -273,52 +327,16 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       phi[1][q] = v[q].y;
     }
     float T6[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
+    kick_tidal<N>(T6, a, b);
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const int r = ra + half;
-      float2* row = psi + b * rg.bstride + (long long)r * rg.pitch;
       const float2* irow = psi_in + b * rg.bstride + (long long)r * rg.pitch;
-      const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
 #pragma unroll
       for (int i = 0; i < N / (R1 * T); ++i)
 #pragma unroll
         for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? irow[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
-      const int y = r % rg.ny, z = r / rg.ny;
-      const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * z;
-      // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2)
-      const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
-      const float lin = T6[3] * fy + T6[4] * fz;
-#pragma unroll
-      for (int i = 0; i < N / (R1 * T); ++i)
-#pragma unroll
-        for (int k = 0; k < R1; ++k) {
-          const int q = i * R1 + k;
-          const int x = slot_pos<N, T, R1>(t, i, k);
-          float pot = phi[half][q];
-          if (a.tidal) {
-            const float fx = a.x0 + a.dx * x;
-            pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
-          }
-          if (a.kerr != 0.f) pot += a.kerr * (v[q].x * v[q].x + v[q].y * v[q].y);
-          if (vrow && ok) pot += vrow[x];
-          v[q] = apply_kick(v[q], pot, a);
-        }
-      if constexpr (FWD) {
-        run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
-        if (ok)
-#pragma unroll
-          for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-            for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
-      } else {
-        if (ok)
-#pragma unroll
-          for (int i = 0; i < N / (R1 * T); ++i)
-#pragma unroll
-            for (int k = 0; k < R1; ++k) row[slot_pos<N, T, R1>(t, i, k)] = v[i * R1 + k];
-      }
+      kick_row<N, FWD>(v, phi[half], T6, a, rg, r, b, ok, psi + b * rg.bstride + (long long)r * rg.pitch, buf, tw, t);
     }
   }
 }
@@ -327,6 +345,47 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
 // P5: psi x-inverse (+mask) of rows A and B, rho = |psi|^2 (+rho_b) - shift,
 // packed R2C of (rho_A, rho_B) -> H rows A and B
 // ----------------------------------------------------------------------------
+// One row of P5: v holds psi row r (write_psi: x-spectral at radix-R1 slots,
+// else real space at radix-RS slots).  Inverts it (+mask) and stores it back
+// to `row` (write_psi), then forms rho - shift at radix-RS slots into rho0
+// (half 0) or the packed z (half 1).  rb: the baryon density row or null.
+template <int N>
+__device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
+                                            float2* row, const float* rb, float shift, int half, float* rho0,
+                                            float2* z, float2* buf, const float4* tw, int t) {
+  using C = XCfg<N>;
+  constexpr int T = C::T;
+  using Rad = typename XPlan<N>::Fwd;
+  constexpr int RS = RadInfo<Rad>::last;
+  if (a.write_psi) {
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
+    if (a.mx) {
+      const int y = r % rg.ny, zz = r / rg.ny;
+      const float myz = ok ? a.my[y] * a.mz[zz] : 0.f;
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) v[i * RS + k] = cscale(v[i * RS + k], myz * a.mx[slot_pos<N, T, RS>(t, i, k)]);
+    }
+    if (ok)
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+  }
+#pragma unroll
+  for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+    for (int k = 0; k < RS; ++k) {
+      const float2 q = v[i * RS + k];
+      float d = q.x * q.x + q.y * q.y;
+      if (ok && a.nonfinite && !isfinite(d)) *a.nonfinite = 1;
+      if (rb && ok) d += rb[slot_pos<N, T, RS>(t, i, k)];
+      if (half == 0) rho0[i * RS + k] = d - shift;
+      else z[i * RS + k] = make_float2(rho0[i * RS + k], d - shift);
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
@@ -350,21 +409,6 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
         for (int i = 0; i < N / (R1 * T); ++i)
 #pragma unroll
           for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
-        run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
-        if (a.mx) {
-          const int y = r % rg.ny, z = r / rg.ny;
-          const float myz = ok ? a.my[y] * a.mz[z] : 0.f;
-#pragma unroll
-          for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-            for (int k = 0; k < RS; ++k)
-              v[i * RS + k] = cscale(v[i * RS + k], myz * a.mx[slot_pos<N, T, RS>(t, i, k)]);
-        }
-        if (ok)
-#pragma unroll
-          for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-            for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
       } else {
 #pragma unroll
         for (int i = 0; i < N / (RS * T); ++i)
@@ -372,17 +416,7 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
           for (int k = 0; k < RS; ++k) v[i * RS + k] = ok ? row[slot_pos<N, T, RS>(t, i, k)] : make_float2(0.f, 0.f);
       }
       const float* rb = a.rho_b ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) {
-          const float2 q = v[i * RS + k];
-          float d = q.x * q.x + q.y * q.y;
-          if (a.nonfinite && !isfinite(d)) *a.nonfinite = 1;
-          if (rb && ok) d += rb[slot_pos<N, T, RS>(t, i, k)];
-          if (half == 0) rho0[i * RS + k] = d - shift;
-          else z[i * RS + k] = make_float2(rho0[i * RS + k], d - shift);
-        }
+      inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t);
     }
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
@@ -639,6 +673,6 @@ k_xw_adj_apply(float2* __restrict__ lam, const float2* __restrict__ Hmu, RowGeom
   }
 }
 
-#undef WDM_XPASS_PROLOGUE
+// WDM_XPASS_PROLOGUE stays defined for the staged kernels (xpass_staged.cuh)
 
 }  // namespace wdm
