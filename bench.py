@@ -107,6 +107,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x, world):
+    """The largest x over the ranks: a job of independent replicas ends with its slowest rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(steps, world, seconds):
+    """Whole-job steps/s of `world` replicas that each ran `steps` steps in `seconds` (the max over ranks)."""
+    return steps * world / seconds
+
+
 def setup_context(wdm, wl, phase_mode, steps_total):
     N, L = wl["n"], wl["L"]
     ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=wl["poisson_coeff"], phase_mode=phase_mode)
@@ -159,11 +176,8 @@ def run_native(args, rank, world):
     ms = ev0.elapsed_time(ev1)
     prof = ctx.profile()
     ctx.set_profiling(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = K * world / (ms / 1e3)
+    ms = max_over_ranks(ms, world)
+    value = replica_throughput(K, world, ms / 1e3)
 
     # e2e: host psi in, one step, psi out, per step (pinned host buffers)
     e2e = None
@@ -186,10 +200,7 @@ def run_native(args, rank, world):
             wdm._abi.check(lib.wdm_step(ctx.handle, 1, dt, 0.0, 0), ctx.handle)
             wdm._abi.check(lib.wdm_get_psi(ctx.handle, C.c_void_p(host_out.data_ptr()), 0), ctx.handle)
         el = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([el], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(el, world)
         nb = psi0.nbytes
         e2e = {"value": ne * world / el, "unit": "steps/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ne, "calls_per_step": ["wdm_set_psi(host)", "wdm_step(1)", "wdm_get_psi(host)"]}
@@ -297,11 +308,8 @@ def run_ensemble(args, rank, world):
     clk = clocks.stop()
     if not all(c.is_finite() for c in ctxs):
         raise RuntimeError("ensemble state became non-finite")
-    if world > 1:
-        t = torch.tensor([el], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
-    value = K * world / el
+    el = max_over_ranks(el, world)
+    value = replica_throughput(K, world, el)
     # per-pass profile from one eager step of each member
     prof = {}
     for c in ctxs:
