@@ -193,12 +193,13 @@ wdm_status wdm_set_profiling(wdm_ctx* ctx, int32_t on);
 wdm_status wdm_get_profile(wdm_ctx* ctx, int64_t* launches, double* ms, double* bytes_per_launch);
 /* Pass schedule chosen by the autotuner when the context was created, for the
  * passes psi-y, psi-z, H-y, H-z (line passes: impl 0 = TMA-fed persistent
- * pass, 1 = register-tile pass) and the kick and density x passes (impl 0 =
- * rows staged by bulk copies, 1 = rows loaded directly), in that order;
- * ms[2k], ms[2k+1] the best timed milliseconds of implementations 0 and 1.
- * The environment variables WDM_LINE_IMPL=tma|tile and
+ * pass, 1 = register-tile pass), the kick, the density pass and the density
+ * pass with baryons (x passes: impl 0 = rows staged by bulk copies, 1 = rows
+ * loaded directly), in that order; ms[2k], ms[2k+1] the best timed
+ * milliseconds of implementations 0 and 1.  The environment variables
+ * WDM_SCHEDULE (all seven, comma separated), WDM_LINE_IMPL=tma|tile and
  * WDM_X_IMPL=staged|direct override the choice. */
-wdm_status wdm_get_line_schedule(const wdm_ctx* ctx, int32_t impl[6], double ms[12]);
+wdm_status wdm_get_line_schedule(const wdm_ctx* ctx, int32_t impl[7], double ms[14]);
 /* number of passes and the name of pass p */
 int32_t wdm_num_passes(void);
 const char* wdm_pass_name(int32_t p);
@@ -207,7 +208,8 @@ int64_t wdm_launch_count(const wdm_ctx* ctx);
 
 /* self-test ------------------------------------------------------------------ */
 /* out[2i], out[2i+1] = sin, cos of h[i] (|h| <= pi/2) as evaluated by the series
- * the precise phase form uses; device pointers, n values. */
+ * the precise phase form uses (the degree-7/8 series for |h| <= 1/4, the
+ * degree-15/16 one above); device pointers, n values. */
 wdm_status wdm_selftest_sincos(const float* h_dev, float* out_dev, int64_t n);
 /* Runs one CTA that waits on an mbarrier nothing completes, through the bounded
  * wait of the TMA-fed passes with a limit of limit_ns nanoseconds.  On return

@@ -303,7 +303,7 @@ def test_pass_implementations_agree(wdm, n, batch, monkeypatch):
         monkeypatch.setenv("WDM_X_IMPL", x_impl)
         with wdm.SPEContext(n, L, poisson_coeff=2.0, kerr=0.3, absorb_alpha=0.5, batch=batch) as ctx:
             sched = ctx.line_schedule()
-            assert [v["impl"] for v in sched.values()] == [line_impl] * 4 + [x_impl] * 2
+            assert [v["impl"] for v in sched.values()] == [line_impl] * 4 + [x_impl] * 3
             ctx.set_psi(psi0)
             ctx.set_tidal(T)
             if batch == 1:
@@ -318,7 +318,7 @@ def test_autotuner_reports_a_schedule(wdm, monkeypatch):
     monkeypatch.delenv("WDM_X_IMPL", raising=False)
     with wdm.SPEContext((64, 64, 64), (1.0, 1.0, 1.0)) as ctx:
         sched = ctx.line_schedule()
-    assert list(sched) == ["psi_y", "psi_z", "h_y", "h_z", "x_kick", "x_rho"]
+    assert list(sched) == ["psi_y", "psi_z", "h_y", "h_z", "x_kick", "x_rho", "x_rho_b"]
     for v in sched.values():
         names = list(v["ms"])
         assert v["impl"] in names

@@ -231,7 +231,8 @@ class SPEContext:
 
     # tuned passes and the names of their two implementations
     SCHEDULE = (("psi_y", ("tma", "tile")), ("psi_z", ("tma", "tile")), ("h_y", ("tma", "tile")),
-                ("h_z", ("tma", "tile")), ("x_kick", ("staged", "direct")), ("x_rho", ("staged", "direct")))
+                ("h_z", ("tma", "tile")), ("x_kick", ("staged", "direct")), ("x_rho", ("staged", "direct")),
+                ("x_rho_b", ("staged", "direct")))
 
     def line_schedule(self):
         """{pass: dict(impl, ms={impl name: best ms})} as chosen by the autotuner at creation."""

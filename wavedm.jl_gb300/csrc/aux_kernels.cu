@@ -8,7 +8,7 @@ namespace wdm {
 __global__ void k_sincos_half(const float* __restrict__ h, float* __restrict__ out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     float s, c;
-    sincos_half(h[i], &s, &c);
+    sincos_half_adaptive(h[i], &s, &c);  // both series: the short one for |h| <= 1/4
     out[2 * i] = s;
     out[2 * i + 1] = c;
   }
@@ -193,8 +193,9 @@ __device__ __forceinline__ long long cic_cell(int ix, int iy, int iz, int nx, in
   return ((long long)iz * ny + iy) * nx + ix;
 }
 
+// rows (ny * nz flags, may be null): set to 1 for every x row a particle touches
 __global__ void k_cic_deposit(float* __restrict__ rho, const CicParticle* __restrict__ p, long long n, int nx, int ny,
-                              int nz) {
+                              int nz, int* __restrict__ rows) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
   const CicParticle a = p[q];
@@ -202,18 +203,23 @@ __global__ void k_cic_deposit(float* __restrict__ rho, const CicParticle* __rest
   for (int c = 0; c < 8; ++c) {
     const int ox = c & 1, oy = (c >> 1) & 1, oz = c >> 2;
     const float w = (ox ? a.f[0] : 1.f - a.f[0]) * (oy ? a.f[1] : 1.f - a.f[1]) * (oz ? a.f[2] : 1.f - a.f[2]);
-    atomicAdd(rho + cic_cell(a.i[0] + ox, a.i[1] + oy, a.i[2] + oz, nx, ny, nz), a.m * w);
+    const long long cell = cic_cell(a.i[0] + ox, a.i[1] + oy, a.i[2] + oz, nx, ny, nz);
+    atomicAdd(rho + cell, a.m * w);
+    if (rows && c % 2 == 0) rows[cell / nx] = 1;
   }
 }
 
 __global__ void k_cic_clear(float* __restrict__ rho, const CicParticle* __restrict__ p, long long n, int nx, int ny,
-                            int nz) {
+                            int nz, int* __restrict__ rows) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
   const CicParticle a = p[q];
 #pragma unroll
-  for (int c = 0; c < 8; ++c)
-    rho[cic_cell(a.i[0] + (c & 1), a.i[1] + ((c >> 1) & 1), a.i[2] + (c >> 2), nx, ny, nz)] = 0.f;
+  for (int c = 0; c < 8; ++c) {
+    const long long cell = cic_cell(a.i[0] + (c & 1), a.i[1] + ((c >> 1) & 1), a.i[2] + (c >> 2), nx, ny, nz);
+    rho[cell] = 0.f;
+    if (rows && c % 2 == 0) rows[cell / nx] = 0;
+  }
 }
 
 __global__ void k_cic_interp(const float* __restrict__ f, const CicParticle* __restrict__ p, long long n, int nx,
@@ -231,16 +237,17 @@ __global__ void k_cic_interp(const float* __restrict__ f, const CicParticle* __r
   out[q] = s;
 }
 
-cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz,
+cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, int* rows,
                                cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  k_cic_deposit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz);
+  k_cic_deposit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz, rows);
   return cudaGetLastError();
 }
 
-cudaError_t launch_cic_clear(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, cudaStream_t st) {
+cudaError_t launch_cic_clear(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, int* rows,
+                             cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  k_cic_clear<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz);
+  k_cic_clear<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz, rows);
   return cudaGetLastError();
 }
 

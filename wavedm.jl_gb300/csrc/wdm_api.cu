@@ -96,7 +96,9 @@ struct Profiler {
 // Line passes the autotuner chooses an implementation for.
 // (the x passes' choice is X_IMPL_STAGED / X_IMPL_DIRECT, the line passes' LINE_IMPL_TMA / LINE_IMPL_TILE;
 // 0 is the preferred implementation of each)
-enum { LP_PSI_Y = 0, LP_PSI_Z = 1, LP_H_Y = 2, LP_H_Z = 3, LP_X_KICK = 4, LP_X_RHO = 5, LP_COUNT = 6 };
+// (LP_X_RHO_B: the density pass with a baryon density to add, which the staged
+// pass prefetches and the direct pass loads after its transform)
+enum { LP_PSI_Y = 0, LP_PSI_Z = 1, LP_H_Y = 2, LP_H_Z = 3, LP_X_KICK = 4, LP_X_RHO = 5, LP_X_RHO_B = 6, LP_COUNT = 7 };
 
 struct wdm_ctx {
   wdm_desc d{};
@@ -119,6 +121,7 @@ struct wdm_ctx {
   double mask_dt = NAN;
   float* V = nullptr;
   float* rho_b = nullptr;
+  int* rb_rows = nullptr;           // ny*nz flags: x rows holding deposited baryon mass
   CicParticle* parts = nullptr;
   long long nparts = 0;
   float* T6b = nullptr;             // per-batch-item tidal tensors
@@ -137,8 +140,8 @@ struct wdm_ctx {
   int phi_valid = 0;
   int64_t launch_count = 0;
   // autotuned implementation of each line pass (LP_*) and the candidate timings
-  int line_impl[LP_COUNT] = {0, 0, 0, 0, 0, 0};
-  double line_ms[LP_COUNT][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
+  int line_impl[LP_COUNT] = {0, 0, 0, 0, 0, 0, 0};
+  double line_ms[LP_COUNT][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
   // adjoint buffers (allocated on first use)
   float2* lam = nullptr;            // adjoint state [batch][ncell]
   float2* Hmu = nullptr;            // half spectrum of mu
@@ -363,7 +366,7 @@ static RowGeom rows_psi(const wdm_ctx* c) {
   return r;
 }
 
-// The rows of psi for the tuned x pass `kind` (LP_X_KICK or LP_X_RHO).
+// The rows of psi for the tuned x pass `kind` (LP_X_KICK, LP_X_RHO or LP_X_RHO_B).
 static RowGeom rows_psi(const wdm_ctx* c, int kind) {
   RowGeom r = rows_psi(c);
   r.impl = c->line_impl[kind];
@@ -412,7 +415,7 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   const int B = c->d.batch;
   if (c->nparts > 0) {
     cudaError_t e = run_pass(c, P_CIC_DEPOSIT, [&] {
-      return launch_cic_deposit(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->st);
+      return launch_cic_deposit(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->rb_rows, c->st);
     });
     if (e != cudaSuccess) return cuda_fail(c, e, "cic deposit");
   }
@@ -423,18 +426,20 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.my = mask ? c->my : nullptr;
   ra.mz = mask ? c->mz : nullptr;
   ra.rho_b = c->nparts > 0 ? c->rho_b : nullptr;
+  ra.rb_rows = c->nparts > 0 ? c->rb_rows : nullptr;
   ra.rb_bstride = 0;
   ra.write_psi = write_psi;
   ra.nonfinite = c->flag;
   ra.shift = c->shift;
   ra.err = c->flag + 1;
   cudaError_t e = run_pass(c, write_psi ? P_X_INV_RHO : P_DENSITY, [&] {
-    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, LP_X_RHO), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
+    return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, c->nparts > 0 ? LP_X_RHO_B : LP_X_RHO), c->hpitch, c->nhalf,
+                            c->twx, ra, B, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
   if (c->nparts > 0) {
     e = run_pass(c, P_CIC_CLEAR, [&] {
-      return launch_cic_clear(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->st);
+      return launch_cic_clear(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->rb_rows, c->st);
     });
     if (e != cudaSuccess) return cuda_fail(c, e, "cic clear");
   }
@@ -607,7 +612,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   if (c->self_group) wdm_group_destroy(c->self_group);
   if (c->st) cudaStreamSynchronize(c->st);
   void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
-                  c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->parts, c->T6b, c->flag, c->scratch_f,
+                  c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->rb_rows, c->parts, c->T6b, c->flag, c->scratch_f,
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -656,15 +661,16 @@ static void forced_impls(wdm_ctx* c) {
   }
   if (const char* env = std::getenv("WDM_X_IMPL")) {
     if (!std::strcmp(env, "staged") || !std::strcmp(env, "direct"))
-      for (int k = LP_X_KICK; k <= LP_X_RHO; ++k)
+      for (int k = LP_X_KICK; k <= LP_X_RHO_B; ++k)
         c->line_impl[k] = std::strcmp(env, "staged") ? X_IMPL_DIRECT : X_IMPL_STAGED;
   }
 }
 
 static wdm_status tune_passes_timed(wdm_ctx* c);
 
-// WDM_SCHEDULE="a,b,c,d,e,f": the whole schedule (psi-y, psi-z, H-y, H-z as
-// tma|tile; kick, density as staged|direct), no timing (e.g. under a profiler).
+// WDM_SCHEDULE="a,b,c,d,e,f,g": the whole schedule (psi-y, psi-z, H-y, H-z as
+// tma|tile; kick, density, density with baryons as staged|direct), no timing
+// (e.g. under a profiler).
 static bool schedule_from_env(wdm_ctx* c) {
   const char* env = std::getenv("WDM_SCHEDULE");
   if (!env) return false;
@@ -727,7 +733,13 @@ static wdm_status tune_passes_timed(wdm_ctx* c) {
       case LP_X_KICK:
         return c->kx->x_kick(c->psi, c->psi, c->H, rows_psi(c, LP_X_KICK), c->hpitch, c->nhalf, c->twx, ka, true, B,
                              c->st);
-      default: return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, LP_X_RHO), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
+      case LP_X_RHO: return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, LP_X_RHO), c->hpitch, c->nhalf, c->twx, ra, B, c->st);
+      default: {
+        // a stand-in baryon density: the zeroed psi buffer, read as floats
+        RhoArgs rb = ra;
+        rb.rho_b = reinterpret_cast<const float*>(c->psi);
+        return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, LP_X_RHO_B), c->hpitch, c->nhalf, c->twx, rb, B, c->st);
+      }
     }
   };
   cudaEvent_t e0, e1;
@@ -940,6 +952,10 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
   if (!c->rho_b) {
     WDM_TRY(dalloc(c, &c->rho_b, (size_t)c->ncell));
     WDM_CU(c, cudaMemsetAsync(c->rho_b, 0, sizeof(float) * c->ncell, c->st));
+  }
+  if (!c->rb_rows) {
+    WDM_TRY(dalloc(c, &c->rb_rows, (size_t)c->d.ny * c->d.nz));
+    WDM_CU(c, cudaMemsetAsync(c->rb_rows, 0, sizeof(int) * c->d.ny * c->d.nz, c->st));
   }
   // cell index and fractions in FP64 on the host (particles are static)
   std::vector<CicParticle> h((size_t)n);

@@ -182,10 +182,19 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     unit_rows(u, C::GROUPS, ppi, &b, &ra);
     stage_rows(slotB, S::PSI_P, psi + b * rg.bstride + ra * rg.pitch, rg.pitch, N, S::ROWS, &xbar[1]);
   };
+  // only the rows flagged as holding baryon mass are copied (a phase with no
+  // copy completes on the arrival alone)
   auto issue_r = [&](long long u) {
     int b, ra;
     unit_rows(u, C::GROUPS, ppi, &b, &ra);
-    stage_rows(rbslot, S::RB_P, a.rho_b + b * a.rb_bstride + ra * rg.pitch, rg.pitch, N, S::ROWS, &xbar[0]);
+    const float* src = a.rho_b + b * a.rb_bstride + ra * rg.pitch;
+    unsigned bytes = 0;
+    for (int r = 0; r < S::ROWS; ++r)
+      if (!a.rb_rows || a.rb_rows[ra + r]) bytes += (unsigned)(N * sizeof(float));
+    mbar_expect_tx(&xbar[0], bytes);
+    for (int r = 0; r < S::ROWS; ++r)
+      if (!a.rb_rows || a.rb_rows[ra + r])
+        bulk_g2s(rbslot + r * S::RB_P, src + r * rg.pitch, (unsigned)(N * sizeof(float)), &xbar[0]);
   };
   const bool with_rb = a.rho_b != nullptr;
   long long u = (long long)blockIdx.x * C::WARPS + warp;
@@ -229,7 +238,8 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       }
       if (half == 0 && with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
       const int r = ra + half;
-      const float* rb = with_rb ? rbslot + (2 * g + half) * S::RB_P : nullptr;
+      const bool rb_row = with_rb && (!a.rb_rows || a.rb_rows[r]);
+      const float* rb = rb_row ? rbslot + (2 * g + half) * S::RB_P : nullptr;
       inv_rho_row<N>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb, shift, half, rho0, z,
                      buf, tw, t);
       if (half == 1 && with_rb) {

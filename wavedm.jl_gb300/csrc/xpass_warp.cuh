@@ -415,7 +415,8 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
 #pragma unroll
           for (int k = 0; k < RS; ++k) v[i * RS + k] = ok ? row[slot_pos<N, T, RS>(t, i, k)] : make_float2(0.f, 0.f);
       }
-      const float* rb = a.rho_b ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
+      const bool rb_row = a.rho_b && (!a.rb_rows || a.rb_rows[r]);  // rows without baryon mass are zero
+      const float* rb = rb_row ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
       inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t);
     }
     reorder<N, T, RS, R1>(z, v);
