@@ -208,8 +208,7 @@ int64_t wdm_launch_count(const wdm_ctx* ctx);
 
 /* self-test ------------------------------------------------------------------ */
 /* out[2i], out[2i+1] = sin, cos of h[i] (|h| <= pi/2) as evaluated by the series
- * the precise phase form uses (the degree-7/8 series for |h| <= 1/4, the
- * degree-15/16 one above); device pointers, n values. */
+ * the precise phase form uses; device pointers, n values. */
 wdm_status wdm_selftest_sincos(const float* h_dev, float* out_dev, int64_t n);
 /* Runs one CTA that waits on an mbarrier nothing completes, through the bounded
  * wait of the TMA-fed passes with a limit of limit_ns nanoseconds.  On return

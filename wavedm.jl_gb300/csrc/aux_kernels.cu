@@ -8,7 +8,7 @@ namespace wdm {
 __global__ void k_sincos_half(const float* __restrict__ h, float* __restrict__ out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     float s, c;
-    sincos_half_adaptive(h[i], &s, &c);  // both series: the short one for |h| <= 1/4
+    sincos_half(h[i], &s, &c);
     out[2 * i] = s;
     out[2 * i + 1] = c;
   }

@@ -490,7 +490,7 @@ __device__ __forceinline__ float2 apply_kick(float2 v, float pot, const KickArgs
     const float te = fmaf(pot, a.dt_hi, -th) + pot * a.dt_lo;
     const float n = rintf(th * 0.15915494309189535f);
     const float r = fmaf(-n, 6.28318548202514648f, th) + fmaf(-n, -1.7484555e-07f, te);
-    const float2 e = expm1_neg_i_small_first(r);  // (cos r - 1, -sin r); kick phases are mostly small
+    const float2 e = expm1_neg_i(r);  // (cos r - 1, -sin r)
     return make_float2(v.x + (v.x * e.x - v.y * e.y), v.y + (v.x * e.y + v.y * e.x));
   }
   sincosf(pot * a.dt_hi, &s, &c);

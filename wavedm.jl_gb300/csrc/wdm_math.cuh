@@ -30,41 +30,11 @@ __device__ __forceinline__ void sincos_half(float h, float* s, float* c) {
   *c = fmaf(x2, pc, 1.f);
 }
 
-// The same series cut at degree 7 (sin) and 8 (cos) for |h| <= 1/4, where the
-// truncation error is below (1/4)^9/9! < 1.1e-11 (relative 4.3e-11) for sin and
-// (1/4)^10/10! < 2.7e-13 for cos: the same FP32 result at half the FMAs.
-__device__ __forceinline__ void sincos_half_small(float h, float* s, float* c) {
-  const float x2 = h * h;
-  float ps = fmaf(x2, -1.9841269841269841270e-4f, 8.3333333333333333333e-3f);  // -1/7!, 1/5!
-  ps = fmaf(x2, ps, -1.6666666666666666667e-1f);                               // -1/3!
-  *s = fmaf(h * x2, ps, h);
-  float pc = fmaf(x2, 2.4801587301587301587e-5f, -1.3888888888888888889e-3f);  // 1/8!, -1/6!
-  pc = fmaf(x2, pc, 4.1666666666666666667e-2f);                                // 1/4!
-  pc = fmaf(x2, pc, -0.5f);                                                    // -1/2!
-  *c = fmaf(x2, pc, 1.f);
-}
-
-// sin/cos of |h| <= pi/2 choosing the short series where it suffices.  For
-// phases that are small across a warp (the kick: dt times the potential), the
-// branch is uniform and half the series is skipped; phases spread over the
-// whole range (the drift) should call sincos_half directly.
-__device__ __forceinline__ void sincos_half_adaptive(float h, float* s, float* c) {
-  if (fabsf(h) <= 0.25f) sincos_half_small(h, s, c);
-  else sincos_half(h, s, c);
-}
-
 // exp(-i r) - 1 = (-2 sin^2(r/2), -2 sin(r/2) cos(r/2)) for |r| <= pi, accurate
 // relative to |exp(-i r) - 1| (no cancellation for small r).
 __device__ __forceinline__ float2 expm1_neg_i(float r) {
   float s, c;
   sincos_half(0.5f * r, &s, &c);
-  return make_float2(-2.f * s * s, -2.f * s * c);
-}
-
-// The same for phases that are usually small (|r| <= 1/2 takes the short series).
-__device__ __forceinline__ float2 expm1_neg_i_small_first(float r) {
-  float s, c;
-  sincos_half_adaptive(0.5f * r, &s, &c);
   return make_float2(-2.f * s * s, -2.f * s * c);
 }
 
