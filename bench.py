@@ -441,8 +441,15 @@ def run_adjoint(args, rank, world):
         loss, _, da = ctx.adjoint(nsteps, dt, rho_d, ckpt_every=ck, tidal_dir=D, grad_out=grad_d)
     t_adj = (time.perf_counter() - t0) / reps
     launches = (ctx.launch_count - l0) // reps
+    # where the adjoint's time goes: one more run with per-pass events (not timed above)
+    ctx.set_psi(psi0)
+    ctx.set_profiling(True)
+    ctx.adjoint(nsteps, dt, rho_d, ckpt_every=ck, tidal_dir=D, grad_out=grad_d)
+    prof = {k: {"launches": v["launches"], "ms": round(v["ms"], 3)} for k, v in ctx.profile().items() if v["launches"]}
+    ctx.set_profiling(False)
     ctx.close()
     return {
+        "passes_adjoint_run": prof,
         "metric": f"adjoint/forward time ratio, {nsteps} Strang steps at {N}^3, checkpoints every {ck}",
         "value": round(t_adj / t_fwd, 3), "unit": "ratio", "n_gpus": world, "steps": nsteps, "warmup": nsteps,
         "ms_per_step": round(t_adj / nsteps * 1e3, 4), "higher_is_better": False, "scaling": "weak",

@@ -75,11 +75,15 @@ enum Pass {
   P_CIC_CLEAR,
   P_X_FFT,         // plain x-FFT (wdm_drift)
   P_PHI_OUT,       // Phi C2R to a real field
+  P_ADJ_KICK,      // adjoint kick: lam x-iFFT, exp(+i th) lam, mu R2C
+  P_ADJ_POISSON,   // Poisson solve of mu (H y, z, y)
+  P_ADJ_APPLY,     // lam += 2 G(mu) psi (+mask), x-FFT
   NPASS
 };
 static const char* const PASS_NAMES[NPASS] = {
     "kick_xfft_fwd", "psi_y_fwd", "psi_z_drift", "psi_y_inv", "psi_x_inv_rho", "rho_y_fwd", "rho_z_poisson",
-    "phi_y_inv",     "kick_final", "rho_density", "cic_deposit", "cic_clear", "psi_x_fwd", "phi_x_c2r"};
+    "phi_y_inv",     "kick_final", "rho_density", "cic_deposit", "cic_clear", "psi_x_fwd", "phi_x_c2r",
+    "adj_kick",   "adj_poisson", "adj_apply"};
 
 struct Profiler {
   bool on = false;
@@ -227,6 +231,9 @@ static double pass_bytes(const wdm_ctx* c, int p) {
     case P_CIC_DEPOSIT: return (double)c->nparts * (sizeof(CicParticle) + 8 * 2 * sizeof(float));
     case P_CIC_CLEAR: return (double)c->nparts * (sizeof(CicParticle) + 8 * sizeof(float));
     case P_PHI_OUT: return 8.0 * nh + 4.0 * nc;
+    case P_ADJ_KICK: return 24.0 * nc + 16.0 * nh;   // lam in/out, pre-kick psi, H in, mu spectrum out
+    case P_ADJ_POISSON: return 3.0 * 16.0 * nh;
+    case P_ADJ_APPLY: return 24.0 * nc + 8.0 * nh;   // lam in/out, pre-kick psi, G(mu) in
     default: return 0.0;
   }
 }
@@ -1380,18 +1387,24 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
       KickArgs ka = kick_args(c, dtk, b);
       j.pre = st_psi(seg, b);
       const float2* Hb = st_H(seg, b);
-      const long long l0 = tl_kernel_launches;
-      if ((e = c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, ka, j, B, c->st)) !=
-          cudaSuccess)
+      if ((e = run_pass(c, P_ADJ_KICK, [&] {
+             return c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, ka, j, B, c->st);
+           })) != cudaSuccess)
         return cuda_fail(c, e, "adjoint kick");
-      if ((e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st)) != cudaSuccess ||
-          (e = c->kz->lfft_poisson(c->Hmu, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st)) != cudaSuccess ||
-          (e = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st)) != cudaSuccess)
+      if ((e = run_pass(c, P_ADJ_POISSON, [&] {
+             cudaError_t f;
+             if ((f = c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st)) !=
+                     cudaSuccess ||
+                 (f = c->kz->lfft_poisson(c->Hmu, lines_z(c, c->nxh, c->hpitch, c->nhalf), c->twz, po, B, c->st)) !=
+                     cudaSuccess)
+               return f;
+             return c->ky->lfft(c->Hmu, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st);
+           })) != cudaSuccess)
         return cuda_fail(c, e, "adjoint Poisson");
-      if ((e = c->kx->adj_apply(c->lam, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, j, b > 0, B, c->st)) !=
-          cudaSuccess)
+      if ((e = run_pass(c, P_ADJ_APPLY, [&] {
+             return c->kx->adj_apply(c->lam, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, j, b > 0, B, c->st);
+           })) != cudaSuccess)
         return cuda_fail(c, e, "adjoint apply");
-      c->launch_count += tl_kernel_launches - l0;
       if (b > 0) WDM_TRY(drift_yz(c, dt, -1.f, c->lam));
     }
   }
