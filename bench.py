@@ -39,6 +39,30 @@ sys.path.insert(0, ROOT)
 
 B_ALG_PER_CELL = 192.0  # 4 C2C 3D FFTs x 3 axis passes x (8 B read + 8 B write) of complex64
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
+# pass, from the ncu captures of the 384^3 workload with the tuned schedule
+# (profiles/step384_kernels.md): (pass, kernel implementation) -> bytes.
+NCU_TRAFFIC_384 = {
+    ("kick_xfft_fwd", "staged"): 1078.1e6,
+    ("kick_final", "staged"): 1077.3e6,
+    ("psi_z_drift", "tma"): 845.1e6,
+    ("psi_x_inv_rho", "staged"): 1091.1e6,
+    ("rho_y_fwd", "tma"): 401.5e6,
+    ("rho_z_poisson", "tma"): 401.6e6,
+    ("phi_y_inv", "tma"): 401.6e6,
+}
+
+
+def ncu_traffic(pass_name, n, workload, sched):
+    """Measured DRAM bytes per launch of the pass when the capture covers this run, else None."""
+    if n != 384 or workload != 3 or not sched:
+        return None
+    impl = {"kick_xfft_fwd": "x_kick", "kick_final": "x_kick", "psi_z_drift": "psi_z", "psi_x_inv_rho": "x_rho_b",
+            "rho_y_fwd": "h_y", "rho_z_poisson": "h_z", "phi_y_inv": "h_y"}.get(pass_name)
+    if impl is None or impl not in sched:
+        return None
+    return NCU_TRAFFIC_384.get((pass_name, sched[impl]["impl"]))
+
 
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -236,7 +260,8 @@ def run_native(args, rank, world):
                    "baryon_particles": 0 if wl["particles"] is None else len(wl["particles"][1]),
                    "l2": "inputs larger than L2 (psi 8 B/cell)", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": ncu_traffic(name, N, args.workload, sched),
                      "bytes_per_launch": p["bytes_per_launch"], "mean_launch_ms": round(mean_ms, 5)},
         "step_effective": {"B_alg_per_cell": B_ALG_PER_CELL,
                            "GBps": round(B_ALG_PER_CELL * ncell * value / world / 1e9, 1),
