@@ -65,19 +65,48 @@ def compare(wdm, wl, steps):
     return out
 
 
+def mass_drift_only(wdm, wl, steps, every=100):
+    """Relative mass drift of both phase forms every `every` steps up to `steps`."""
+    N, L, dt = wl["n"], wl["L"], wl["dt"]
+    psi0 = wl["psi0"].astype(np.complex64)
+    sched = wl["tidal"](np.arange(steps + 2) * dt) if wl.get("tidal") is not None else None
+    out = {"n": N, "L": L, "dt": dt, "steps": steps, "every": every}
+    for mode in ("precise", "plain"):
+        with wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=wl["poisson_coeff"], phase_mode=mode) as ctx:
+            ctx.set_psi(psi0)
+            if wl.get("particles") is not None:
+                ctx.set_particles(*wl["particles"])
+            m0 = ctx.reduce()["mass"]
+            drift = []
+            for s0 in range(0, steps, every):
+                k = min(every, steps - s0)
+                if sched is not None:
+                    ctx.set_tidal(sched[s0: s0 + k + 1])
+                ctx.step(k, dt, t0=s0 * dt)
+                drift.append(float(ctx.reduce()["mass"] / m0 - 1.0))
+        out[mode] = {"mass_drift": drift[-1], "mass_drift_every": drift}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", type=int, required=True, choices=[1, 2, 3, 4])
     ap.add_argument("--steps", type=int, default=None, help="default: the workload's own step count")
     ap.add_argument("--n", type=int, default=None, help="override the grid size")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--gpu-only", action="store_true",
+                    help="no oracle: the mass drift of both phase forms over the step count (the FP64 path conserves "
+                         "mass to ~1e-13, so the drift needs no reference run)")
     a = ap.parse_args()
 
     import wavedm_gb300 as wdm
 
     wdm.build_library()
     report = {"workload": a.workload}
-    if a.workload == 4:
+    if a.gpu_only and a.workload != 4:
+        wl = wdm.ics.workload(a.workload, n=a.n)
+        report.update(mass_drift_only(wdm, wl, a.steps or wl["steps"]))
+    elif a.workload == 4:
         seen = set()
         report["halos"] = []
         for N, L, psi0, T6 in wdm.ics.ensemble_members():
