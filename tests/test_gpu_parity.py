@@ -325,3 +325,17 @@ def test_autotuner_reports_a_schedule(wdm, monkeypatch):
         assert all(0 < t < 1e3 for t in v["ms"].values())
         faster = names[1] if v["ms"][names[1]] < 0.97 * v["ms"][names[0]] else names[0]
         assert v["impl"] == faster
+
+
+@pytest.mark.parametrize("n,c,steps", [(96, 1.0, 300), (192, 0.0, 200)], ids=["96-gravity", "192-free"])
+def test_precise_phases_conserve_mass(wdm, n, c, steps):
+    """Mass conservation of the precise form at sizes with a factor 3 (radix-3
+    and radix-6 stages): |M(T)/M(0) - 1| <= 1e-6 per run, the criterion of the
+    accuracy claims (measured ~1e-7 here)."""
+    w = wdm.ics.workload(1, n=n)
+    with wdm.SPEContext((n, n, n), (w["L"],) * 3, poisson_coeff=c, phase_mode="precise") as ctx:
+        ctx.set_psi(w["psi0"].astype(np.complex64))
+        m0 = ctx.reduce()["mass"]
+        ctx.step(steps, w["dt"])
+        m1 = ctx.reduce()["mass"]
+    assert abs(m1 / m0 - 1) < 1e-6
