@@ -91,3 +91,33 @@ def test_adjoint_workload5_shape_at_64(wdm):
     drc = float(np.real(np.sum(np.conj(grad.astype(np.complex128)) * dpsi)))
     drc_ref = float(np.real(np.sum(np.conj(g_ref) * dpsi)))
     assert drc == pytest.approx(drc_ref, rel=1e-3)
+
+
+ADJ_IMPL_CASES = [(32, 24, 16), (64, 16, 8), (128, 16, 16), (96, 8, 8)]
+
+
+@pytest.mark.parametrize("n", ADJ_IMPL_CASES, ids=["x".join(map(str, n)) for n in ADJ_IMPL_CASES])
+def test_adjoint_kick_implementations_agree(wdm, n, monkeypatch):
+    """The staged adjoint kick (rows copied to shared memory one unit ahead) and
+    the direct one share their arithmetic: forced onto either, an adjoint run
+    with tide, Kerr term and absorbing mask gives bit-identical gradients."""
+    L = (4.0, 3.0, 5.0)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    rng = np.random.default_rng(8)
+    shape = (n[2], n[1], n[0])
+    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2)) * np.exp(1j * rng.uniform(0, 1, shape)) + 0.01).astype(np.complex64)
+    target = (0.5 * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 1.5)).astype(np.float32)
+    D = np.array([2.0, -1.0, -1.0, 0.1, 0.0, 0.0])
+    out = {}
+    for x_impl in ("staged", "direct"):
+        monkeypatch.setenv("WDM_X_IMPL", x_impl)
+        with wdm.SPEContext(n, L, poisson_coeff=2.0, kerr=0.3, absorb_alpha=0.5) as ctx:
+            ctx.set_psi(psi0)
+            ctx.set_tidal([0.02 * D])
+            out[x_impl] = ctx.adjoint(6, 0.01, target, ckpt_every=4, tidal_dir=D)
+    # the loss and dL/da are FP64 sums of per-block partials added atomically,
+    # so only their last bits depend on the order the blocks finish in
+    assert out["staged"][0] == pytest.approx(out["direct"][0], rel=1e-12)
+    assert np.array_equal(out["staged"][1], out["direct"][1])
+    assert out["staged"][2] == pytest.approx(out["direct"][2], rel=1e-12)

@@ -23,6 +23,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace wdm {
 
@@ -212,18 +213,54 @@ struct RadInfo<Radices<Rs...>> {
 // stages
 // ----------------------------------------------------------------------------
 // Twiddle W = (x, y) + (z, w): FP32 nearest value plus its FP32 remainder
-// from the FP64 value, so the rotation is exact up to one rounding of the
+// from the FP64 value, so the rotation is exact up to the rounding of the
 // result.  A plain FP32 table rounds each |W| slightly off 1 in a fixed way
 // and the mean of those errors compounds into a mass drift step after step.
-// The small correction terms are formed first and the large products are
-// added last: a correction added to an already rounded FP32 product is
-// smaller than half its ulp and would round straight back, leaving the
-// twiddle's modulus error (and the drift it causes) in place.
+//
+// The remainder terms are small, below half an ulp of the result, so they
+// survive only if they are added inside an FMA whose product is not already
+// on the FP32 grid: there the exact sum falls at a random place between grid
+// points and the rounding keeps the correction on average.  Both components
+// are therefore formed as fma(outer, fma(inner, corrections)) with the inner
+// product on the y part of W.  That part must not be exactly +-1/2 (the only
+// value between 0 and 1 in magnitude that cos/sin of a rational angle takes
+// on the grid): a*(1/2) is exact, the correction would round away and
+// |W| would act as its uncompensated FP32 value.  Entries with sin = +-1/2
+// (angles of 30 degrees mod 180, present once 3 divides the length) are
+// stored as i W instead, flagged in the last bit of the y remainder, and
+// rotate the input by -i (forward) or +i (inverse) to match:
+// a W = (-i a)(i W), a conj(W) = (i a) conj(i W).
+__host__ __device__ inline float4 pack_twiddle(double c, double s) {
+  float hx = (float)c, hy = (float)s;
+  float lx = (float)(c - (double)hx), ly = (float)(s - (double)hy);
+  unsigned flag = 0;
+  if (hy == 0.5f || hy == -0.5f) {
+    const float tx = hx, tl = lx;
+    hx = -hy;
+    lx = -ly;
+    hy = tx;
+    ly = tl;
+    flag = 1;
+  }
+  unsigned bits;
+  memcpy(&bits, &ly, sizeof(bits));
+  bits = (bits & ~1u) | flag;  // moves the remainder by at most one of its ulps
+  memcpy(&ly, &bits, sizeof(bits));
+  return make_float4(hx, hy, lx, ly);
+}
+
+// ROT: the stage's table can hold flagged entries.  A stage twiddles by
+// W_{NS R}^m, and sin = +-1/2 needs an angle of 30 degrees mod 180, so only
+// stages with 12 | NS R can; the others skip the flag test.
+template <bool ROT>
 __device__ __forceinline__ float2 twiddle_mul(float2 a, float4 w, bool inv) {
+  const bool rot = ROT && (__float_as_uint(w.w) & 1u) != 0;
+  const float ax = rot ? (inv ? -a.y : a.y) : a.x;
+  const float ay = rot ? (inv ? a.x : -a.x) : a.y;
   const float wy = inv ? -w.y : w.y, ly = inv ? -w.w : w.w;
-  const float cx = fmaf(a.x, w.z, -a.y * ly);
-  const float cy = fmaf(a.x, ly, a.y * w.z);
-  return make_float2(fmaf(a.x, w.x, fmaf(-a.y, wy, cx)), fmaf(a.x, wy, fmaf(a.y, w.x, cy)));
+  const float cx = fmaf(ax, w.z, -ay * ly);
+  const float cy = fmaf(ax, ly, ay * w.z);
+  return make_float2(fmaf(ax, w.x, fmaf(-ay, wy, cx)), fmaf(ay, w.x, fmaf(ax, wy, cy)));
 }
 
 // Stage twiddles are laid out per stage as [jm][k-1] (jm < NS, 1 <= k < R),
@@ -242,7 +279,7 @@ __device__ __forceinline__ void stage_compute(float2* v, const float4* __restric
       const int jm = j % NS;
       const float4* w = tw + OFF + jm * (R - 1);
 #pragma unroll
-      for (int k = 1; k < R; ++k) v[i * R + k] = twiddle_mul(v[i * R + k], w[k - 1], INV);
+      for (int k = 1; k < R; ++k) v[i * R + k] = twiddle_mul<(NS * R) % 12 == 0>(v[i * R + k], w[k - 1], INV);
     }
     dftR<R, INV>(v + i * R);
   }

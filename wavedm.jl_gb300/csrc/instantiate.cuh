@@ -165,12 +165,12 @@ struct Launch {
     return true;
   }
   template <auto K>
-  static dim3 grid_xs(const RowGeom& rg, int batch, XWork* w) {
+  static dim3 grid_xs(const RowGeom& rg, int batch, XWork* w, size_t smem = XS::SMEM) {
     w->pairs_per_item = rg.nrows / 2;
     w->batch = batch;
     const long long units = (long long)w->pairs_per_item * batch / XCfg<N>::GROUPS;
     const long long ctas = (units + XCfg<N>::WARPS - 1) / XCfg<N>::WARPS;
-    const long long cap = (long long)resident_ctas<K>(XNT, XS::SMEM) * sm_count();
+    const long long cap = (long long)resident_ctas<K>(XNT, smem) * sm_count();
     return dim3((unsigned)(ctas < cap ? ctas : cap));
   }
   static cudaError_t x_inv_rho(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
@@ -240,9 +240,7 @@ struct Launch {
   static void fill_twiddles(float4* out) {
     auto make = [](long long m) {
       const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)N;
-      const double cr = std::cos(a), ci = std::sin(a);
-      const float hr = (float)cr, hi = (float)ci;
-      return make_float4(hr, hi, (float)(cr - (double)hr), (float)(ci - (double)hi));
+      return pack_twiddle(std::cos(a), std::sin(a));
     };
     for (int q = 0; q < TW_TABLES * N; ++q) out[q] = make_float4(1.f, 0.f, 0.f, 0.f);
     using LF = typename Plan<N>::Fwd;
@@ -257,6 +255,18 @@ struct Launch {
                               cudaStream_t st) {
     cudaError_t e;
     XWork w;
+    // staged where its three slots still leave 3 or more CTAs per SM
+    using XA = XStageAdj<N>;
+    if constexpr (XA::MINB_RAW >= 3) {
+      if (x_staged_ok(rg, hpitch, lam, H, j.pre)) {
+        constexpr auto K = k_xs_adj_kick<N>;
+        if ((e = prep_once<K>(XA::SMEM)) != cudaSuccess) return e;
+        const dim3 gr = grid_xs<K>(rg, batch, &w, XA::SMEM);
+        K<<<gr, XNT, XA::SMEM, st>>>(lam, H, Hmu, rg, hpitch, hbstride, tw, a, j, w);
+        ++tl_kernel_launches;
+        return cudaGetLastError();
+      }
+    }
     const dim3 gr = grid_x(rg, batch, &w);
     if ((e = prep_once<k_xw_adj_kick<N>>(XSMEM)) != cudaSuccess) return e;
     k_xw_adj_kick<N><<<gr, XNT, XSMEM, st>>>(lam, H, Hmu, rg, hpitch, hbstride, tw, a, j, w);

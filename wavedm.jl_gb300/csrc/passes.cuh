@@ -483,18 +483,34 @@ struct KickArgs {
 // psi + psi (exp(-i r) - 1) with exp(-i r) - 1 = (-2 sin^2(r/2), -sin r) from the
 // series sin/cos of r/2 (wdm_math.cuh): accurate relative to |exp(-i r) - 1|, so
 // small kicks do not carry the fixed modulus error of a cosine rounded near 1.
-__device__ __forceinline__ float2 apply_kick(float2 v, float pot, const KickArgs& a) {
-  float s, c;
+// kick_factor gives the phase factor once, so that a caller applying the same
+// kick to two states (the adjoint: psi and lam) evaluates it once:
+// exp(-i r) - 1 in the precise form, exp(-i th) in the plain form.
+__device__ __forceinline__ float2 kick_factor(float pot, const KickArgs& a) {
   if (a.precise) {
     const float th = pot * a.dt_hi;
     const float te = fmaf(pot, a.dt_hi, -th) + pot * a.dt_lo;
     const float n = rintf(th * 0.15915494309189535f);
     const float r = fmaf(-n, 6.28318548202514648f, th) + fmaf(-n, -1.7484555e-07f, te);
-    const float2 e = expm1_neg_i(r);  // (cos r - 1, -sin r)
-    return make_float2(v.x + (v.x * e.x - v.y * e.y), v.y + (v.x * e.y + v.y * e.x));
+    return expm1_neg_i(r);  // (cos r - 1, -sin r)
   }
+  float s, c;
   sincosf(pot * a.dt_hi, &s, &c);
-  return cmul(v, make_float2(c, -s));
+  return make_float2(c, -s);
+}
+
+// v exp(-i th), or v exp(+i th) (CONJ), from the factor of kick_factor.  In
+// the precise form the conjugate factor is bit for bit the factor of -pot (the
+// reduction and the series are odd/even in th), so CONJ is a kick by -pot.
+template <bool CONJ = false>
+__device__ __forceinline__ float2 kick_by(float2 v, float2 e, const KickArgs& a) {
+  if (CONJ) e.y = -e.y;
+  if (a.precise) return make_float2(v.x + (v.x * e.x - v.y * e.y), v.y + (v.x * e.y + v.y * e.x));
+  return cmul(v, e);
+}
+
+__device__ __forceinline__ float2 apply_kick(float2 v, float pot, const KickArgs& a) {
+  return kick_by(v, kick_factor(pot, a), a);
 }
 
 }  // namespace wdm

@@ -73,12 +73,11 @@ wdm_status scratch_on_current_device(unsigned char** out) {
   return WDM_OK;
 }
 
-// W_N^m as an FP32 (hi, lo) pair from the FP64 value.
+// W_N^m as an FP32 (hi, lo) pair from the FP64 value (pack_twiddle layout).
 __device__ float4 twiddle_entry(long long m, int n) {
   double s, c;
   sincospi(-2.0 * (double)m / (double)n, &s, &c);
-  const float hr = (float)c, hi = (float)s;
-  return make_float4(hr, hi, (float)(c - (double)hr), (float)(s - (double)hi));
+  return pack_twiddle(c, s);
 }
 
 // Entry idx of the stage-major table of a radix order (same layout as

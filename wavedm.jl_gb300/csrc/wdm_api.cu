@@ -152,7 +152,10 @@ struct wdm_ctx {
   float* rho_t = nullptr;           // target density
   float* D6 = nullptr;              // tidal direction
   double* adj_acc = nullptr;        // [2 batch]: loss, dL/da
-  std::vector<float2*> ck_psi, ck_H, slot_psi, slot_H;  // checkpoints / segment states
+  std::vector<float2*> ck_psi, ck_H, slot_psi, slot_H;  // checkpoints / segment states (set 0)
+  std::vector<float2*> slot2_psi, slot2_H;              // segment states, set 1
+  cudaStream_t st_rec = nullptr;    // adjoint: recompute of the next segment, beside the reverse sweep
+  cudaEvent_t ev_ck = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_bwd[2] = {nullptr, nullptr};
   long long version = 0;            // bumped by every set_* call that a captured graph bakes in
   struct wdm_group* self_group = nullptr;  // single-member group of wdm_step_graph
   Profiler prof;
@@ -618,6 +621,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   if (!c) return WDM_OK;
   if (c->self_group) wdm_group_destroy(c->self_group);
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->st_rec) cudaStreamSynchronize(c->st_rec);
   void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
                   c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->rb_rows, c->parts, c->T6b, c->flag, c->scratch_f,
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
@@ -626,9 +630,12 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc};
   for (void* p : adj)
     if (p) cudaFree(p);
-  for (auto* v : {&c->ck_psi, &c->ck_H, &c->slot_psi, &c->slot_H})
+  for (auto* v : {&c->ck_psi, &c->ck_H, &c->slot_psi, &c->slot_H, &c->slot2_psi, &c->slot2_H})
     for (float2* p : *v)
       if (p) cudaFree(p);
+  if (c->st_rec) cudaStreamDestroy(c->st_rec);
+  for (cudaEvent_t e : {c->ev_ck, c->ev_rec[0], c->ev_rec[1], c->ev_bwd[0], c->ev_bwd[1]})
+    if (e) cudaEventDestroy(e);
   for (auto& r : c->prof.pending) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -1326,8 +1333,28 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   if (!c->D6) WDM_TRY(dalloc(c, &c->D6, 6));
   if (!c->adj_acc) WDM_TRY(dalloc(c, &c->adj_acc, (size_t)2 * B));
   const int nck = nsteps / ck + 1;
+  const int last_seg = (nsteps - 1) / ck, jl0 = last_seg * ck;
+  // Segment s keeps its states in slot set s % 2.  The recompute of segment
+  // s - 1 (on st_rec) then runs beside the reverse sweep of segment s (on the
+  // context stream): each alone leaves most of the GPU idle at small grids.
   WDM_TRY(ensure_pairs(c, c->ck_psi, c->ck_H, (size_t)nck));
   WDM_TRY(ensure_pairs(c, c->slot_psi, c->slot_H, (size_t)ck + 1));
+  if (last_seg > 0) {
+    WDM_TRY(ensure_pairs(c, c->slot2_psi, c->slot2_H, (size_t)ck + 1));
+    if (!c->st_rec) WDM_CU(c, cudaStreamCreateWithFlags(&c->st_rec, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c->ev_ck, &c->ev_rec[0], &c->ev_rec[1], &c->ev_bwd[0], &c->ev_bwd[1]})
+      if (!*e) WDM_CU(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  // on every way out, later work on the context stream waits for st_rec (on an
+  // early error return it may still hold recomputes that use the scratch buffers)
+  struct Join {
+    wdm_ctx* c;
+    ~Join() {
+      if (c->st_rec && cudaEventRecord(c->ev_ck, c->st_rec) == cudaSuccess) cudaStreamWaitEvent(c->st, c->ev_ck, 0);
+    }
+  } join{c};
+  std::vector<float2*>* set_psi[2] = {&c->slot_psi, &c->slot2_psi};
+  std::vector<float2*>* set_H[2] = {&c->slot_H, &c->slot2_H};
   WDM_TRY(copy_in(c, c->rho_t, rho_target, sizeof(float) * nc, where_t));
   if (tidal_dir) {
     float d6[6];
@@ -1339,11 +1366,12 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   if (c->d.absorb_alpha != 0.0) WDM_TRY(ensure_mask_tables(c, dt));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
   // forward: checkpoints of (s_b, H_b) at b = 0, ck, 2 ck, ...; the states of
-  // the last segment go straight into the slots (no recompute needed for it)
-  const int last_seg = (nsteps - 1) / ck, jl0 = last_seg * ck;
-  // state s_b of the segment starting at j0: the checkpoint or a slot
-  auto st_psi = [&](int seg, int b) { return b == seg * ck ? c->ck_psi[seg] : c->slot_psi[b - seg * ck]; };
-  auto st_H = [&](int seg, int b) { return b == seg * ck ? c->ck_H[seg] : c->slot_H[b - seg * ck]; };
+  // the last segment go straight into its slots (no recompute needed for it)
+  // state s_b of the segment starting at j0: the checkpoint or a slot of its set
+  auto st_psi = [&](int seg, int b) {
+    return b == seg * ck ? c->ck_psi[seg] : (*set_psi[seg & 1])[b - seg * ck];
+  };
+  auto st_H = [&](int seg, int b) { return b == seg * ck ? c->ck_H[seg] : (*set_H[seg & 1])[b - seg * ck]; };
   WDM_TRY(copy_pair(c, c->ck_psi[0], c->ck_H[0], c->psi, c->H));
   for (int b = 0; b < jl0; ++b) {
     WDM_TRY(forward_boundary(c, b, dt));
@@ -1375,20 +1403,46 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   po.ky2 = c->ky2;
   po.kz2 = c->kz2;
   po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
+  // recompute s_{j0+1..j1} of segment seg into its slots, out of place, on st_rec
+  auto recompute = [&](int seg) -> wdm_status {
+    const int j0 = seg * ck, j1 = std::min(j0 + ck, nsteps);
+    cudaStream_t keep = c->st;
+    c->st = c->st_rec;
+    wdm_status s = WDM_OK;
+    for (int b = j0; b < j1 && s == WDM_OK; ++b)
+      s = forward_boundary_to(c, b, dt, st_psi(seg, b), st_H(seg, b), st_psi(seg, b + 1), st_H(seg, b + 1));
+    cudaError_t er = cudaSuccess;
+    if (s == WDM_OK) er = cudaEventRecord(c->ev_rec[seg & 1], c->st_rec);
+    c->st = keep;
+    if (er != cudaSuccess) return cuda_fail(c, er, "adjoint recompute event");
+    return s;
+  };
+  if (last_seg > 0) {
+    // recomputes start from the checkpoints of the forward run above
+    WDM_CU(c, cudaEventRecord(c->ev_ck, c->st));
+    WDM_CU(c, cudaStreamWaitEvent(c->st_rec, c->ev_ck, 0));
+    WDM_TRY(recompute(last_seg - 1));
+  }
   for (int seg = last_seg; seg >= 0; --seg) {
     const int j0 = seg * ck, j1 = std::min(j0 + ck, nsteps);
-    // recompute s_{j0+1..j1} of this segment into the slots, out of place
-    if (seg != last_seg)
-      for (int b = j0; b < j1; ++b)
-        WDM_TRY(forward_boundary_to(c, b, dt, st_psi(seg, b), st_H(seg, b), st_psi(seg, b + 1), st_H(seg, b + 1)));
+    if (seg != last_seg) {
+      WDM_CU(c, cudaStreamWaitEvent(c->st, c->ev_rec[seg & 1], 0));  // this segment's states
+      if (seg > 0) {
+        // segment seg - 1 reuses the slots of segment seg + 1, whose sweep is done
+        WDM_CU(c, cudaStreamWaitEvent(c->st_rec, c->ev_bwd[(seg + 1) & 1], 0));
+        WDM_TRY(recompute(seg - 1));
+      }
+    }
     const int blo = (j0 == 0) ? 0 : j0 + 1;
     for (int b = j1; b >= blo; --b) {
       const double dtk = (b == 0 || b == nsteps) ? 0.5 * dt : dt;
       KickArgs ka = kick_args(c, dtk, b);
       j.pre = st_psi(seg, b);
       const float2* Hb = st_H(seg, b);
+      // the adjoint kick follows the kick pass's implementation (staged or direct)
       if ((e = run_pass(c, P_ADJ_KICK, [&] {
-             return c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c), c->hpitch, c->nhalf, c->twx, ka, j, B, c->st);
+             return c->kx->adj_kick(c->lam, Hb, c->Hmu, rows_psi(c, LP_X_KICK), c->hpitch, c->nhalf, c->twx, ka, j,
+                                    B, c->st);
            })) != cudaSuccess)
         return cuda_fail(c, e, "adjoint kick");
       if ((e = run_pass(c, P_ADJ_POISSON, [&] {
@@ -1407,6 +1461,7 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
         return cuda_fail(c, e, "adjoint apply");
       if (b > 0) WDM_TRY(drift_yz(c, dt, -1.f, c->lam));
     }
+    if (seg >= 2) WDM_CU(c, cudaEventRecord(c->ev_bwd[seg & 1], c->st));  // its slots may be reused
   }
   // leave the context at psi_0 with its potential
   WDM_TRY(copy_pair(c, c->psi, c->H, c->ck_psi[0], c->ck_H[0]));

@@ -60,8 +60,20 @@ __device__ __forceinline__ void xrelease() {
   __syncwarp();
 }
 
-#define WDM_XSTAGE_PROLOGUE                                                                          \
-  using S = XStage<N>;                                                                               \
+// The adjoint kick stages a third slot, the pre-kick rows, after slot B; its
+// lam and pre rows complete on the one barrier of slot B.
+template <int N>
+struct XStageAdj : XStage<N> {
+  using B = XStage<N>;
+  static constexpr size_t WARP_BYTES = B::A_BYTES + 2 * B::B_BYTES;
+  static constexpr size_t SMEM = B::BASE + B::C::WARPS * WARP_BYTES + B::C::WARPS * 2 * sizeof(uint64_t);
+  static constexpr int MINB_RAW = (int)((228u * 1024u) / (SMEM + 1024u));
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+};
+
+#define WDM_XSTAGE_PROLOGUE WDM_XSTAGE_PROLOGUE_T(XStage<N>)
+#define WDM_XSTAGE_PROLOGUE_T(ST)                                                                    \
+  using S = ST;                                                                                      \
   unsigned char* sraw = reinterpret_cast<unsigned char*>(smem);                                      \
   unsigned char* wslots = sraw + S::BASE + (size_t)warp * S::WARP_BYTES;                             \
   float2* slotA = reinterpret_cast<float2*>(wslots);                                                 \
@@ -257,8 +269,105 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
   }
 }
 
+// Adjoint kick (staged): the arithmetic of k_xw_adj_kick, with the H rows in
+// slot A and the lam and pre rows of the unit in slots B and C, all copied
+// one unit ahead.  The updated lam rows and the packed mu spectrum are stored
+// straight to global memory.
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, XStageAdj<N>::MINB)
+k_xs_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __restrict__ Hmu, RowGeom rg,
+              long long hpitch, long long hbstride, const float4* __restrict__ twg, KickArgs a, AdjArgs j,
+              XWork w) {
+  WDM_XPASS_PROLOGUE
+  WDM_XSTAGE_PROLOGUE_T(XStageAdj<N>)
+  float2* slotC = slotB + S::ROWS * S::PSI_P;
+  auto issue_h = [&](long long u) {
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    stage_rows(slotA, S::H_P, H + b * hbstride + ra * hpitch, hpitch, S::HP, S::ROWS, &xbar[0]);
+  };
+  auto issue_lp = [&](long long u) {
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    const unsigned rb = (unsigned)(N * sizeof(float2));
+    const long long o = b * rg.bstride + ra * rg.pitch;
+    mbar_expect_tx(&xbar[1], 2u * rb * (unsigned)S::ROWS);
+    for (int r = 0; r < S::ROWS; ++r) {
+      bulk_g2s(slotB + r * S::PSI_P, lam + o + r * rg.pitch, rb, &xbar[1]);
+      bulk_g2s(slotC + r * S::PSI_P, j.pre + o + r * rg.pitch, rb, &xbar[1]);
+    }
+  };
+  long long u = (long long)blockIdx.x * C::WARPS + warp;
+  if (u < nunits) {
+    if (lane == 0) {
+      issue_h(u);
+      issue_lp(u);
+    }
+    pend = 3u;
+  }
+  for (; u < nunits; u += wstride) {
+    const long long un = u + wstride;
+    int b, ra;
+    unit_rows(u, C::GROUPS, ppi, &b, &ra);
+    ra += 2 * g;  // this lane group's pair
+    if (!WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
+    float2 v[N / T];
+    load_packed_half<N, T, R1>(v, slotA + (2 * g) * S::H_P, slotA + (2 * g + 1) * S::H_P, true, t);
+    xrelease();
+    if (un < nunits) {
+      if (lane == 0) issue_h(un);
+      pend |= 1u;
+    }
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
+    float phi[2][N / T];
+#pragma unroll
+    for (int q = 0; q < N / T; ++q) {
+      phi[0][q] = v[q].x;
+      phi[1][q] = v[q].y;
+    }
+    float T6[6];
+    kick_tidal<N>(T6, a, b);
+    float mu0[N / T];
+    float2 z[N / T];
+    float damp = 0.f;
+    if (!WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int r = ra + half;
+      const float2* lrow = slotB + (2 * g + half) * S::PSI_P;
+      const float2* prow = slotC + (2 * g + half) * S::PSI_P;
+      float2* row = lam + b * rg.bstride + (long long)r * rg.pitch;
+      const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) v[i * R1 + k] = lrow[slot_pos<N, T, R1>(t, i, k)];
+      run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // lam+ in real space, radix-RS slots
+      auto pre_at = [&](int, int x) { return prow[x]; };
+      adj_kick_points<N>(v, phi[half], pre_at, vrow, T6, a, j, rg, r, true, row, half, mu0, z, damp, t);
+      if (half == 1) {
+        xrelease();
+        if (un < nunits) {
+          if (lane == 0) issue_lp(un);
+          pend |= 2u;
+        }
+      }
+    }
+    reorder<N, T, RS, R1>(z, v);
+    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
+    float2* hm = Hmu + b * hbstride + ra * hpitch;
+    store_packed_half<N, T, RS>(v, buf, hm, hm + hpitch, true, t);
+    if (j.D6) {
+#pragma unroll
+      for (int off = T / 2; off > 0; off >>= 1) damp += __shfl_down_sync(0xffffffffu, damp, off, T);
+      if (t == 0) atomicAdd(j.damp + b, (double)damp);
+    }
+  }
+}
+
 #undef WDM_XSTAGE_FAIL
 #undef WDM_XSTAGE_WAIT
+#undef WDM_XSTAGE_PROLOGUE_T
 #undef WDM_XSTAGE_PROLOGUE
 #undef WDM_XPASS_PROLOGUE
 

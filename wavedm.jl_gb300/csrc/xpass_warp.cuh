@@ -16,6 +16,11 @@
 #ifndef WDM_X_MINB
 #define WDM_X_MINB 4
 #endif
+// largest points per lane at which the adjoint kick loads the lam and pre
+// rows of its pair ahead into registers (0: never)
+#ifndef WDM_ADJ_PF
+#define WDM_ADJ_PF 8
+#endif
 
 namespace wdm {
 
@@ -528,11 +533,67 @@ struct AdjArgs {
   const float* mz;
 };
 
+// Pointwise part of the adjoint kick for row r, shared by the direct and the
+// staged kernel: v holds lam+ at the radix-RS slots, phi the potential there
+// and pre_at(q, x) the pre-kick state at slot q (position x).  Stores the new
+// lam row (when ok), keeps mu of row A in mu0 and packs (mu_A, mu_B) into z
+// at row B, and adds the tidal-amplitude term of the row to damp.
+template <int N, class PreAt>
+__device__ __forceinline__ void adj_kick_points(const float2* v, const float* phi, PreAt pre_at, const float* vrow,
+                                                const float* T6, const KickArgs& a, const AdjArgs& j,
+                                                const RowGeom& rg, int r, bool ok, float2* row, int half, float* mu0,
+                                                float2* z, float& damp, int t) {
+  using C = XCfg<N>;
+  constexpr int T = C::T;
+  constexpr int RS = RadInfo<typename XPlan<N>::Fwd>::last;
+  const int y = r % rg.ny, zc = r / rg.ny;
+  const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * zc;
+  const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
+  const float lin = T6[3] * fy + T6[4] * fz;
+  float dyz = 0.f, dlin = 0.f;
+  if (j.D6) {
+    dyz = 0.5f * j.D6[1] * fy * fy + j.D6[5] * fy * fz + 0.5f * j.D6[2] * fz * fz;
+    dlin = j.D6[3] * fy + j.D6[4] * fz;
+  }
+#pragma unroll
+  for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+    for (int k = 0; k < RS; ++k) {
+      const int q = i * RS + k;
+      const int x = slot_pos<N, T, RS>(t, i, k);
+      const float2 pre = pre_at(q, x);
+      const float fx = a.x0 + a.dx * x;
+      float pot = phi[q];
+      if (a.tidal) pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
+      if (a.kerr != 0.f) pot += a.kerr * (pre.x * pre.x + pre.y * pre.y);
+      if (vrow && ok) pot += vrow[x];
+      // mu = dt Im(conj(lam+) psi+) with psi+ = exp(-i th) pre equals
+      // dt Im(conj(exp(+i th) lam+) pre): the rotated lam serves both
+      float2 ln = kick_by<true>(v[q], kick_factor(pot, a), a);  // exp(+i th) lam+
+      const float mu = a.dt_hi * (ln.x * pre.y - ln.y * pre.x);
+      if (a.kerr != 0.f) {
+        ln.x = fmaf(2.f * a.kerr * mu, pre.x, ln.x);
+        ln.y = fmaf(2.f * a.kerr * mu, pre.y, ln.y);
+      }
+      if (j.D6) damp = fmaf(mu, fmaf(fx, fmaf(0.5f * j.D6[0], fx, dlin), dyz), damp);
+      if (ok) row[x] = ln;
+      if (half == 0)
+        mu0[q] = mu;
+      else
+        z[q] = make_float2(mu0[q], mu);
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __restrict__ Hmu, RowGeom rg,
               long long hpitch, long long hbstride, const float4* __restrict__ twg, KickArgs a, AdjArgs j, XWork w) {
   WDM_XPASS_PROLOGUE
+  // With at most WDM_ADJ_PF points per lane the lam and pre rows of the pair
+  // fit in registers: row A's are loaded before the potential transform, row
+  // B's after it, so the warp does not wait on them one by one.
+  constexpr bool PF = N / T <= WDM_ADJ_PF;
+  constexpr int PN = PF ? N / T : 1;
   for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
     const long long pp = u * C::GROUPS + g;
     const bool ok = pp < (long long)w.pairs_per_item * w.batch;
@@ -542,6 +603,23 @@ k_xw_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __
     float2 v[N / T];
     // potential rows of the pair, at the radix-RS slots
     load_packed_half<N, T, R1>(v, hrow, hrow + hpitch, ok, t);
+    // lam rows at the radix-R1 slots, pre rows at the radix-RS slots
+    float2 lpf[2][PN], ppf[2][PN];
+    auto prefetch = [&](int half) {
+      const float2* row = lam + b * rg.bstride + (long long)(ra + half) * rg.pitch;
+      const float2* prow = j.pre + b * rg.bstride + (long long)(ra + half) * rg.pitch;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k)
+          lpf[half][i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k)
+          ppf[half][i * RS + k] = ok ? prow[slot_pos<N, T, RS>(t, i, k)] : make_float2(0.f, 0.f);
+    };
+    if constexpr (PF) prefetch(0);
     run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
     float phi[2][N / T];
 #pragma unroll
@@ -549,6 +627,7 @@ k_xw_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __
       phi[0][q] = v[q].x;
       phi[1][q] = v[q].y;
     }
+    if constexpr (PF) prefetch(1);
     float T6[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
@@ -561,45 +640,23 @@ k_xw_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __
       float2* row = lam + b * rg.bstride + (long long)r * rg.pitch;
       const float2* prow = j.pre + b * rg.bstride + (long long)r * rg.pitch;
       const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
+      if constexpr (PF) {
 #pragma unroll
-      for (int i = 0; i < N / (R1 * T); ++i)
+        for (int q = 0; q < N / T; ++q) v[q] = lpf[half][q];
+      } else {
 #pragma unroll
-        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
-      run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // lam+ in real space, radix-RS slots
-      const int y = r % rg.ny, zc = r / rg.ny;
-      const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * zc;
-      const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
-      const float lin = T6[3] * fy + T6[4] * fz;
-      float dyz = 0.f, dlin = 0.f;
-      if (j.D6) {
-        dyz = 0.5f * j.D6[1] * fy * fy + j.D6[5] * fy * fz + 0.5f * j.D6[2] * fz * fz;
-        dlin = j.D6[3] * fy + j.D6[4] * fz;
+        for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+          for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? row[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
       }
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) {
-          const int q = i * RS + k;
-          const int x = slot_pos<N, T, RS>(t, i, k);
-          const float2 pre = ok ? prow[x] : make_float2(0.f, 0.f);
-          const float fx = a.x0 + a.dx * x;
-          float pot = phi[half][q];
-          if (a.tidal) pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
-          if (a.kerr != 0.f) pot += a.kerr * (pre.x * pre.x + pre.y * pre.y);
-          if (vrow && ok) pot += vrow[x];
-          const float2 post = apply_kick(pre, pot, a);
-          const float2 lp = v[q];
-          const float mu = a.dt_hi * (lp.x * post.y - lp.y * post.x);
-          float2 ln = apply_kick(lp, -pot, a);  // exp(+i th) lam+
-          if (a.kerr != 0.f) {
-            ln.x = fmaf(2.f * a.kerr * mu, pre.x, ln.x);
-            ln.y = fmaf(2.f * a.kerr * mu, pre.y, ln.y);
-          }
-          if (j.D6) damp = fmaf(mu, fmaf(fx, fmaf(0.5f * j.D6[0], fx, dlin), dyz), damp);
-          if (ok) row[x] = ln;
-          if (half == 0) mu0[q] = mu;
-          else z[q] = make_float2(mu0[q], mu);
-        }
+      run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // lam+ in real space, radix-RS slots
+      auto pre_at = [&](int q, int x) {
+        if constexpr (PF)
+          return ppf[half][q];
+        else
+          return ok ? prow[x] : make_float2(0.f, 0.f);
+      };
+      adj_kick_points<N>(v, phi[half], pre_at, vrow, T6, a, j, rg, r, ok, row, half, mu0, z, damp, t);
     }
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
