@@ -23,6 +23,8 @@
  *   SPE3D_waveDM loop body    src/simulation_main.jl:536-559 -> wdm_step
  *   add_tidal_potential!      src/physics/tidal_fields.jl:64-118 -> wdm_set_tidal
  *   total mass / virial sums  src/simulation_main.jl:652, src/visualization/runtime.jl:210-238 -> wdm_reduce
+ *   loop diagnostics (findmax, radii quantiles, R, momentum) and compute_timestep limits
+ *                             src/simulation_main.jl:551-558,641-653, src/physics/poisson.jl:35-50 -> wdm_diagnostics
  */
 #ifndef WAVEDM_H
 #define WAVEDM_H
@@ -177,6 +179,31 @@ wdm_status wdm_adjoint(wdm_ctx* ctx, int32_t nsteps, double dt, int32_t ckpt_eve
  * centre of mass x, y, z, and the virial sums VirialPotential, TotalKineticE,
  * TotalQuantumE, Virial = 2K + 2Q - VirialPotential */
 wdm_status wdm_reduce(wdm_ctx* ctx, double* out);
+/* The per-step loop diagnostics of src/simulation_main.jl:551-558,641-653 and
+ * the timestep limits of compute_timestep (src/physics/poisson.jl:35-50),
+ * computed on the device so the loop needs no psi download.
+ * out[WDM_DIAG_FIELDS * b + k] for batch item b:
+ *   0..9   the wdm_reduce fields;
+ *   10..12 MomentumX/Y/Z = sum rho v dV over interior cells
+ *          (src/visualization/runtime.jl:229-231, code units);
+ *   13     max |Phi| (gravity with baryons; the tidal term is not included);
+ *   14     max |psi|;
+ *   15..17 the limits 2 dx^2 / pi, 2 pi / max|Phi|, 2 pi / (|kappa| max|psi|)
+ *          (infinity where a denominator is zero);
+ *   18     R: weighted standard deviation (uncorrected, weights |psi|^2) of
+ *          the distance from the coordinate origin over the z-slice nz/2 - 1
+ *          (0-based; the reference's r[:, :, div(end, 2)]);
+ *   19..27 radii at p = 0.1, 0.2, ..., 0.9: weighted quantiles of the distance
+ *          from the density maximum with weights rho (the StatsBase weighted
+ *          quantile, FP64 cumulative sums; needs dx == dy == dz, else NaN). */
+#define WDM_DIAG_FIELDS 28
+wdm_status wdm_diagnostics(wdm_ctx* ctx, double* out);
+/* The weighted quantile behind the radii, on values grouped by equal value:
+ * groups ascending strictly in value[], with the total weight wsum[] and the
+ * smallest element weight wmin[] of each group (empty groups: wsum 0).
+ * Host-only; the grouped form of StatsBase's quantile(v, w, p). */
+wdm_status wdm_weighted_quantiles_grouped(const double* value, const double* wsum, const double* wmin, int64_t ngroups,
+                                          const double* p, int32_t np, double* out);
 /* CIC interpolation of Phi (gravity) at n positions [n][3] -> out[n] (doubles, host) */
 wdm_status wdm_interpolate_phi(wdm_ctx* ctx, const double* pos, int64_t n, double* out);
 /* 1 if the last checked step left psi finite */

@@ -369,6 +369,100 @@ def virial_terms(psi, phi, grid: Grid):
     }
 
 
+def weighted_quantile(v, w, p):
+    """Weighted quantiles of ``v`` at probabilities ``p`` with weights ``w``.
+
+    Restates StatsBase's ``quantile(v, w::AbstractWeights, p)`` for weights other
+    than FrequencyWeights (StatsBase compat "0.34", ``Project.toml:103``; called
+    as ``quantile(r_mass_center[:], weights(rho[:]), 0.1:0.1:0.9)`` at
+    ``src/simulation_main.jl:641``), element by element:
+    zero weights are dropped; the pairs (v, w) are sorted; with S_k the
+    cumulative weight and h = p (sum w - w_1) + w_1, the first k with S_k > h
+    gives v_{k-1} + (h - S_{k-1}) / (S_k - S_{k-1}) (v_k - v_{k-1}), where v_0 = 0
+    and S_0 = 0; when no S_k exceeds h the result is the largest v.
+    Cumulative sums are FP64 here; the reference accumulates in the weights'
+    element type.
+    """
+    v = np.asarray(v, np.float64).ravel()
+    w = np.asarray(w, np.float64).ravel()
+    keep = w != 0
+    v, w = v[keep], w[keep]
+    order = np.lexsort((w, v))
+    v, w = v[order], w[order]
+    S = np.cumsum(w)
+    total, w1 = S[-1], w[0]
+    out = []
+    for pp in np.atleast_1d(p):
+        h = pp * (total - w1) + w1
+        k = int(np.searchsorted(S, h, side="right"))
+        if k >= len(v):
+            out.append(v[-1])
+            continue
+        vprev = v[k - 1] if k else 0.0
+        sprev = S[k - 1] if k else 0.0
+        out.append(vprev + (h - sprev) / (S[k] - sprev) * (v[k] - vprev))
+    return np.array(out)
+
+
+def loop_diagnostics(psi, phi, grid: Grid, kappa=0.0):
+    """The per-step host diagnostics of the reference loop, restated in FP64.
+
+    * ``rho_max, rho_max_id = findmax(rho)`` and the distances from that cell,
+      ``r_mass_center`` (``src/simulation_main.jl:553-555``; first maximum in
+      x-fastest order);
+    * ``R = std(r[:, :, div(end, 2)], aweights(|psi|^2 on that slice))``
+      (``:558``), with r the distance from the coordinate origin and the
+      uncorrected weighted variance (StatsBase's default for ``std`` with
+      weights);
+    * the radii ``quantile(r_mass_center[:], weights(rho[:]), 0.1:0.1:0.9)``
+      (``:641``) by ``weighted_quantile``;
+    * momentum sums of ``src/visualization/runtime.jl:229-231`` (interior cells,
+      as ``virial_terms``);
+    * the timestep limits of ``compute_timestep`` (``src/physics/poisson.jl:35-50``):
+      2 dx^2/pi, 2 pi / max|Phi|, 2 pi / (|kappa| max|psi|).
+    """
+    rho = np.abs(psi) ** 2
+    nz, ny, nx = rho.shape
+    arg = int(np.argmax(rho))
+    cz, rem = divmod(arg, nx * ny)
+    cy, cx = divmod(rem, nx)
+    X, Y, Z = grid.coords()
+    dx, dy, dz = grid.spacing
+    if np.isclose(dx, dy, rtol=1e-12, atol=0) and np.isclose(dx, dz, rtol=1e-12, atol=0):
+        # cubic cells: distances from integer cell offsets, so equal distances
+        # tie exactly (FP64 coordinate differences would break such ties by
+        # rounding noise and make the tie order, which the interpolation at a
+        # group's first element depends on, arbitrary)
+        i = np.arange(nx)[None, None, :] - cx
+        j = np.arange(ny)[None, :, None] - cy
+        k = np.arange(nz)[:, None, None] - cz
+        r_mc = dx * np.sqrt((i * i + j * j + k * k).astype(np.float64))
+    else:
+        r_mc = np.sqrt((X - X[0, 0, cx]) ** 2 + (Y - Y[0, cy, 0]) ** 2 + (Z - Z[cz, 0, 0]) ** 2)
+    zs = max(nz // 2 - 1, 0)
+    r0 = np.sqrt(X[0] ** 2 + Y[0] ** 2 + Z[zs] ** 2)
+    w0 = rho[zs]
+    mean = np.sum(w0 * r0) / np.sum(w0)
+    R = np.sqrt(np.sum(w0 * (r0 - mean) ** 2) / np.sum(w0))
+    vt = virial_terms(psi, phi, grid)
+    phimax = float(np.max(np.abs(phi)))
+    psimax = float(np.sqrt(rho.max()))
+    return {
+        "rho_max": float(rho.max()),
+        "argmax": arg,
+        "R": float(R),
+        "radii": weighted_quantile(r_mc, rho, np.arange(1, 10) / 10.0),
+        "MomentumX": vt["MomentumX"],
+        "MomentumY": vt["MomentumY"],
+        "MomentumZ": vt["MomentumZ"],
+        "phi_abs_max": phimax,
+        "psi_abs_max": psimax,
+        "dt_phase": 2 * dx * dx / np.pi,
+        "dt_grav": 2 * np.pi / phimax if phimax > 0 else np.inf,
+        "dt_self": 2 * np.pi / abs(kappa) / psimax if kappa != 0 and psimax > 0 else np.inf,
+    }
+
+
 def spectral_energy(psi, grid: Grid, phys: Physics, t=0.0):
     """Total energy E = 1/2 sum |grad psi|^2 dV + 1/2 sum rho Phi_grav dV + sum rho V_ext dV."""
     dV = grid.dV

@@ -3,6 +3,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -73,3 +74,30 @@ def test_null_arguments_are_errors(wdm):
 def test_python_api_fails_loudly_without_library(wdm, tmp_path):
     with pytest.raises(ImportError):
         wdm._abi.load(str(tmp_path / "missing.so"))
+
+
+def test_grouped_weighted_quantile_matches_the_oracle(wdm):
+    """The library's host-side quantile over groups of equal values (the form the
+    device histogram of the radii gives) equals the oracle's element-wise
+    StatsBase restatement on data with many ties and zero weights."""
+    from oracle import spe
+
+    rng = np.random.default_rng(5)
+    for trial in range(20):
+        vals = np.sort(rng.choice(np.arange(1, 200) * 0.37, size=rng.integers(1, 40), replace=False))
+        v = rng.choice(vals, size=rng.integers(1, 400))
+        w = rng.exponential(size=v.size) * (rng.random(v.size) > 0.1)
+        if not np.any(w > 0):
+            continue
+        groups = np.unique(v)
+        wsum = np.array([w[v == u].sum() for u in groups])
+        wmin = np.array([w[(v == u) & (w > 0)].min() if np.any((v == u) & (w > 0)) else 0.0 for u in groups])
+        p = np.concatenate([[0.0, 1.0], rng.random(30)])
+        got = wdm.weighted_quantiles_grouped(groups, wsum, wmin, p)
+        ref = spe.weighted_quantile(v, w, p)
+        assert np.allclose(got, ref, rtol=1e-12, atol=1e-12), trial
+
+
+def test_grouped_weighted_quantile_rejects_unsorted_groups(wdm):
+    with pytest.raises(wdm._abi.WdmError):
+        wdm.weighted_quantiles_grouped([1.0, 1.0], [1.0, 1.0], [1.0, 1.0], [0.5])

@@ -187,3 +187,45 @@ def test_virial_terms_plane_wave():
     assert v["TotalKineticE"] == pytest.approx(0.5 * j * j * nint * g.dV, rel=1e-12)
     assert abs(v["TotalQuantumE"]) < 1e-20
     assert v["MomentumX"] == pytest.approx(j * nint * g.dV, rel=1e-12)
+
+
+def test_weighted_quantile_equal_weights_is_type7_quantile():
+    """StatsBase documents that with equal weights the weighted quantile is the
+    unweighted one (Hyndman-Fan type 7, numpy's default 'linear')."""
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=257)
+    p = np.linspace(0.0, 1.0, 21)
+    got = spe.weighted_quantile(v, np.full(v.size, 0.37), p)
+    assert np.allclose(got, np.quantile(v, p), rtol=0, atol=1e-12)
+
+
+def test_weighted_quantile_hand_example():
+    """v = (1, 2, 3, 4), w = (2, 1, 1, 4): S = (2, 3, 4, 8), w_1 = 2,
+    h = p (8 - 2) + 2.  p = 0.5: h = 5 -> first S_k > 5 is S_4 = 8, so
+    3 + (5 - 4)/(8 - 4) (4 - 3) = 3.25.  p = 0.1: h = 2.6 -> S_2 = 3,
+    1 + 0.6 (2 - 1) = 1.6.  p = 0: h = 2 -> S_2 = 3 > 2, 1 + 0 = 1.
+    p = 1: h = 8 -> no S_k > 8, the largest value 4.  A zero weight drops out."""
+    v = np.array([4.0, 2.0, 9.0, 1.0, 3.0])
+    w = np.array([4.0, 1.0, 0.0, 2.0, 1.0])
+    got = spe.weighted_quantile(v, w, [0.5, 0.1, 0.0, 1.0])
+    assert np.allclose(got, [3.25, 1.6, 1.0, 4.0], rtol=0, atol=1e-15)
+
+
+def test_loop_diagnostics_of_a_gaussian():
+    """Radii about the maximum of a centred Gaussian blob grow with p, R of
+    the middle slice is positive, a plane-wave factor gives the momentum of
+    virial_terms and the timestep limits follow compute_timestep."""
+    n, L = (24, 24, 24), (6.0, 6.0, 6.0)
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    k = 2 * np.pi / L[0]
+    psi = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 2) * np.exp(1j * k * X)
+    phi = -np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 4)
+    d = spe.loop_diagnostics(psi, phi, g, kappa=0.5)
+    assert np.all(np.diff(d["radii"]) > 0) and d["radii"][0] > 0
+    assert d["argmax"] == np.argmax(np.abs(psi) ** 2)
+    assert d["R"] > 0
+    assert d["MomentumX"] == pytest.approx(spe.virial_terms(psi, phi, g)["MomentumX"], rel=1e-14)
+    assert d["dt_phase"] == pytest.approx(2 * g.spacing[0] ** 2 / np.pi)
+    assert d["dt_grav"] == pytest.approx(2 * np.pi / np.abs(phi).max())
+    assert d["dt_self"] == pytest.approx(2 * np.pi / 0.5 / np.abs(psi).max())

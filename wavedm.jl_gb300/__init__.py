@@ -7,9 +7,10 @@ operator API (``solver``: apply_kick_step, apply_drift_step, parallel_poisson,
 SPE3D_waveDM, ...) and the seeded workload generators (``ics``).
 """
 from . import _abi, ics  # noqa: F401
-from .core import Ensemble, SPEContext, size_supported  # noqa: F401
+from .core import Ensemble, SPEContext, size_supported, weighted_quantiles_grouped  # noqa: F401
 
-__all__ = ["SPEContext", "Ensemble", "size_supported", "ics", "build_library", "lib_path"]
+__all__ = ["SPEContext", "Ensemble", "size_supported", "weighted_quantiles_grouped", "ics", "build_library",
+           "lib_path"]
 
 
 def build_library(force=False, verbose=False):

@@ -66,6 +66,8 @@ SIGNATURES = [
     ("wdm_fft3d", _i32, [_vp, _vp, _i32]),
     ("wdm_poisson_noalloc", _i32, [_vp, _vp, _i32, _i32, _i32, _d, _d, _d, _d, _vp]),
     ("wdm_reduce", _i32, [_vp, _vp]),
+    ("wdm_diagnostics", _i32, [_vp, _vp]),
+    ("wdm_weighted_quantiles_grouped", _i32, [_vp, _vp, _vp, _i64, _vp, _i32, _vp]),
     ("wdm_interpolate_phi", _i32, [_vp, _vp, _i64, _vp]),
     ("wdm_check_finite", _i32, [_vp, C.POINTER(_i32)]),
     ("wdm_stream", _vp, [_vp]),

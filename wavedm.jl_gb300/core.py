@@ -198,6 +198,19 @@ class SPEContext:
         recs = [dict(zip(self.FIELDS, row.tolist())) for row in out]
         return recs[0] if self.batch == 1 else recs
 
+    DIAG_FIELDS = FIELDS + ("MomentumX", "MomentumY", "MomentumZ", "phi_abs_max", "psi_abs_max",
+                            "dt_phase", "dt_grav", "dt_self", "R") + tuple(f"radius_{k}0" for k in range(1, 10))
+
+    def diagnostics(self):
+        """The loop diagnostics of the reference's SPE3D_waveDM (mass, density maximum
+        and its index, Lagrangian radii about it, R, virial and momentum sums) and
+        the compute_timestep limits, on the device (wdm_diagnostics)."""
+        n = len(self.DIAG_FIELDS)
+        out = np.zeros((self.batch, n), np.float64)
+        self._check(self.lib.wdm_diagnostics(self.handle, C.c_void_p(out.ctypes.data)))
+        recs = [dict(zip(self.DIAG_FIELDS, row.tolist())) for row in out]
+        return recs[0] if self.batch == 1 else recs
+
     def interpolate_phi(self, pos):
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         out = np.zeros(len(pos), np.float64)
@@ -296,6 +309,20 @@ class Ensemble:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def weighted_quantiles_grouped(value, wsum, wmin, p):
+    """The library's grouped weighted quantile (host code, no GPU): groups of equal
+    value ascending, with total and smallest element weight per group."""
+    lib = _abi.load()
+    value = np.ascontiguousarray(value, np.float64)
+    wsum = np.ascontiguousarray(wsum, np.float64)
+    wmin = np.ascontiguousarray(wmin, np.float64)
+    p = np.ascontiguousarray(p, np.float64)
+    out = np.zeros(len(p), np.float64)
+    check(lib.wdm_weighted_quantiles_grouped(value.ctypes.data, wsum.ctypes.data, wmin.ctypes.data, len(value),
+                                             p.ctypes.data, len(p), out.ctypes.data))
+    return out
 
 
 def size_supported(n):

@@ -106,7 +106,8 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
   for (int q = 0; q < RED_FIELDS; ++q) acc[q] = 0.0;
   acc[RED_MAX] = -1.0;
   acc[RED_ARG] = 0.0;
-  const double i2dx = 0.5 / g.dx, i2dy = 0.5 / g.dy, i2dz = 0.5 / g.dz;
+  acc[RED_PHIMAX] = 0.0;
+  const float fi2dx = (float)(0.5 / g.dx), fi2dy = (float)(0.5 / g.dy), fi2dz = (float)(0.5 / g.dz);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int z = (int)(i / nxy);
     const long long rem = i - z * nxy;
@@ -122,23 +123,40 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
       acc[RED_MAX] = rho;
       acc[RED_ARG] = (double)i;
     }
+    const double ph = (double)phi[i];
+    acc[RED_PHIMAX] = fmax(acc[RED_PHIMAX], fabs(ph));
+    if (z == g.zmid) {
+      const double fx = g.x0 + g.dx * x, fy = g.y0 + g.dy * y, fz = g.z0 + g.dz * z;
+      const double r2 = fx * fx + fy * fy + fz * fz;
+      acc[RED_SW] += rho;
+      acc[RED_SWR] += rho * sqrt(r2);
+      acc[RED_SWR2] += rho * r2;
+    }
     if (x > 0 && x < g.nx - 1 && y > 0 && y < g.ny - 1 && z > 0 && z < g.nz - 1) {
-      acc[RED_W] += rho * (double)phi[i];
+      // Per-cell terms in FP32 (the reference forms them from its FP32 psi
+      // too); every sum accumulates in FP64.  FP64 arithmetic per cell (six
+      // square roots) made this kernel compute-bound on this GPU's FP64 units.
+      const float rf = fmaf(p.x, p.x, p.y * p.y);
+      acc[RED_W] += (double)(rf * phi[i]);
       const float2 xp = psi[i + 1], xm = psi[i - 1];
       const float2 yp = psi[i + g.nx], ym = psi[i - g.nx];
       const float2 zp = psi[i + nxy], zm = psi[i - nxy];
       // rho v = Im(conj(psi) grad psi)
-      const double gxr = (xp.x - xm.x) * i2dx, gxi = (xp.y - xm.y) * i2dx;
-      const double gyr = (yp.x - ym.x) * i2dy, gyi = (yp.y - ym.y) * i2dy;
-      const double gzr = (zp.x - zm.x) * i2dz, gzi = (zp.y - zm.y) * i2dz;
-      const double jx = p.x * gxi - p.y * gxr;
-      const double jy = p.x * gyi - p.y * gyr;
-      const double jz = p.x * gzi - p.y * gzr;
-      if (rho > 0) acc[RED_K] += (jx * jx + jy * jy + jz * jz) / rho;
-      const double ax = (sqrt((double)xp.x * xp.x + (double)xp.y * xp.y) - sqrt((double)xm.x * xm.x + (double)xm.y * xm.y)) * i2dx;
-      const double ay = (sqrt((double)yp.x * yp.x + (double)yp.y * yp.y) - sqrt((double)ym.x * ym.x + (double)ym.y * ym.y)) * i2dy;
-      const double az = (sqrt((double)zp.x * zp.x + (double)zp.y * zp.y) - sqrt((double)zm.x * zm.x + (double)zm.y * zm.y)) * i2dz;
-      acc[RED_Q] += ax * ax + ay * ay + az * az;
+      const float gxr = (xp.x - xm.x) * fi2dx, gxi = (xp.y - xm.y) * fi2dx;
+      const float gyr = (yp.x - ym.x) * fi2dy, gyi = (yp.y - ym.y) * fi2dy;
+      const float gzr = (zp.x - zm.x) * fi2dz, gzi = (zp.y - zm.y) * fi2dz;
+      const float jx = fmaf(p.x, gxi, -p.y * gxr);
+      const float jy = fmaf(p.x, gyi, -p.y * gyr);
+      const float jz = fmaf(p.x, gzi, -p.y * gzr);
+      acc[RED_PX] += (double)jx;
+      acc[RED_PY] += (double)jy;
+      acc[RED_PZ] += (double)jz;
+      if (rf > 0.f) acc[RED_K] += (double)(fmaf(jx, jx, fmaf(jy, jy, jz * jz)) / rf);
+      auto mag = [](float2 v) { return sqrtf(fmaf(v.x, v.x, v.y * v.y)); };
+      const float ax = (mag(xp) - mag(xm)) * fi2dx;
+      const float ay = (mag(yp) - mag(ym)) * fi2dy;
+      const float az = (mag(zp) - mag(zm)) * fi2dz;
+      acc[RED_Q] += (double)fmaf(ax, ax, fmaf(ay, ay, az * az));
     }
   }
   // block reduction (warp shuffles, then one warp over the warp results)
@@ -149,7 +167,8 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
 #pragma unroll
     for (int q = 0; q < RED_FIELDS; ++q) {
       const double o = __shfl_down_sync(0xffffffffu, acc[q], off);
-      if (q == RED_MAX || q == RED_ARG) continue;
+      if (q == RED_PHIMAX) acc[q] = fmax(acc[q], o);
+      if (red_is_max(q)) continue;
       acc[q] += o;
     }
     const double om = __shfl_down_sync(0xffffffffu, acc[RED_MAX], off);
@@ -169,7 +188,8 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
     for (int q = 0; q < RED_FIELDS; ++q) r[q] = sh[0][q];
     for (int k = 1; k < RED_THREADS / 32; ++k) {
       for (int q = 0; q < RED_FIELDS; ++q)
-        if (q != RED_MAX && q != RED_ARG) r[q] += sh[k][q];
+        if (!red_is_max(q)) r[q] += sh[k][q];
+      r[RED_PHIMAX] = fmax(r[RED_PHIMAX], sh[k][RED_PHIMAX]);
       if (sh[k][RED_MAX] > r[RED_MAX] || (sh[k][RED_MAX] == r[RED_MAX] && sh[k][RED_ARG] < r[RED_ARG])) {
         r[RED_MAX] = sh[k][RED_MAX];
         r[RED_ARG] = sh[k][RED_ARG];
@@ -183,6 +203,36 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
 cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g, double* partials, int nblocks,
                           int batch, cudaStream_t st) {
   k_reduce<<<dim3(nblocks, batch), RED_THREADS, 0, st>>>(psi, phi, g, partials);
+  return cudaGetLastError();
+}
+
+// Weights of the distances from the density maximum (the weighted quantiles of
+// src/simulation_main.jl:641-650), keyed by the squared distance in cells.
+// Cells of zero density take no part, as zero weights take none in the
+// weighted quantile.
+__global__ void k_radii_hist(const float2* __restrict__ psi, int nx, int ny, int nz, int cx, int cy, int cz,
+                             double* __restrict__ wsum, unsigned long long* __restrict__ wmin) {
+  const long long nxy = (long long)nx * ny, n = nxy * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = psi[i];
+    const double rho = (double)p.x * p.x + (double)p.y * p.y;
+    if (!(rho > 0.0)) continue;
+    const int z = (int)(i / nxy);
+    const long long rem = i - z * nxy;
+    const int y = (int)(rem / nx);
+    const int x = (int)(rem - (long long)y * nx);
+    const long long ddx = x - cx, ddy = y - cy, ddz = z - cz;
+    const long long key = ddx * ddx + ddy * ddy + ddz * ddz;
+    atomicAdd(&wsum[key], rho);
+    atomicMin(&wmin[key], (unsigned long long)__double_as_longlong(rho));
+  }
+}
+
+cudaError_t launch_radii_hist(const float2* psi, int nx, int ny, int nz, int cx, int cy, int cz, double* wsum,
+                              unsigned long long* wmin, cudaStream_t st) {
+  const long long n = (long long)nx * ny * nz;
+  const long long b = (n + 255) / 256;
+  k_radii_hist<<<(unsigned)(b < 152 * 16 ? b : 152 * 16), 256, 0, st>>>(psi, nx, ny, nz, cx, cy, cz, wsum, wmin);
   return cudaGetLastError();
 }
 

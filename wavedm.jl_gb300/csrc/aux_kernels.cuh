@@ -23,13 +23,29 @@ enum {
   RED_W,         // sum rho Phi over interior cells
   RED_K,         // sum (rho v)^2 / rho over interior cells
   RED_Q,         // sum |grad sqrt rho|^2 over interior cells
+  RED_PX,        // sum rho v (= Im(conj(psi) grad psi)) over interior cells
+  RED_PY,
+  RED_PZ,
+  RED_PHIMAX,    // max |Phi|
+  RED_SW,        // z-slice zmid: sum rho, sum rho r, sum rho r^2 (r from the coordinate origin)
+  RED_SWR,
+  RED_SWR2,
   RED_FIELDS
 };
+// fields combined by max rather than by sum (RED_ARG travels with RED_MAX)
+__host__ __device__ constexpr bool red_is_max(int q) { return q == RED_MAX || q == RED_ARG || q == RED_PHIMAX; }
 
 struct RedGeom {
   int nx, ny, nz;
   double dx, dy, dz, x0, y0, z0;
+  int zmid;  // z index of the slice the RED_SW* sums cover
 };
+
+// Lagrangian radii: per squared cell distance key = di^2 + dj^2 + dk^2 from
+// cell (cx, cy, cz), the FP64 sum of rho and the smallest nonzero rho (as the
+// bits of a positive double) over the cells at that distance.
+cudaError_t launch_radii_hist(const float2* psi, int nx, int ny, int nz, int cx, int cy, int cz, double* wsum,
+                              unsigned long long* wmin, cudaStream_t st);
 
 cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t st);
 // Adjoint seed of L = sum (|psi|^2 - rho_t)^2 dV: lam = 4 (|psi|^2 - rho_t) psi dV,

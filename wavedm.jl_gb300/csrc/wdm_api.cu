@@ -1,6 +1,8 @@
 // C-ABI of libwavedm: context, tables, step orchestration, diagnostics, CIC.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1109,9 +1111,9 @@ wdm_status wdm_fft3d(wdm_ctx* c, void* data, int32_t dir) {
   return WDM_OK;
 }
 
-wdm_status wdm_reduce(wdm_ctx* c, double* out) {
-  WDM_TRY(need_psi(c));
-  if (!out) return fail(c, WDM_ERR_INVALID, "null output");
+// The per-item FP64 reduction of psi and Phi (k_reduce), block partials
+// combined on the host: r[b] holds the RED_* fields of batch item b.
+static wdm_status reduce_items(wdm_ctx* c, std::vector<std::array<double, RED_FIELDS>>& r) {
   WDM_TRY(phi_real(c));
   RedGeom g;
   g.nx = c->d.nx;
@@ -1123,41 +1125,183 @@ wdm_status wdm_reduce(wdm_ctx* c, double* out) {
   g.x0 = c->x0;
   g.y0 = c->y0;
   g.z0 = c->z0;
+  g.zmid = c->d.nz / 2 - 1 > 0 ? c->d.nz / 2 - 1 : 0;  // the slice div(end, 2) of a 1-based z axis
   cudaError_t e = launch_reduce(c->psi, c->scratch_f, g, c->red, c->red_blocks, c->d.batch, c->st);
   if (e != cudaSuccess) return cuda_fail(c, e, "reduce");
   std::vector<double> h((size_t)c->red_blocks * RED_FIELDS * c->d.batch);
   WDM_CU(c, cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
   WDM_CU(c, cudaStreamSynchronize(c->st));
-  const double dV = c->dx * c->dy * c->dz;
+  r.assign((size_t)c->d.batch, {});
   for (int b = 0; b < c->d.batch; ++b) {
-    double acc[RED_FIELDS] = {0};
-    double best = -1.0, besti = 0;
+    std::array<double, RED_FIELDS>& acc = r[(size_t)b];
+    acc.fill(0.0);
+    acc[RED_MAX] = -1.0;
     for (int k = 0; k < c->red_blocks; ++k) {
-      const double* r = &h[((size_t)b * c->red_blocks + k) * RED_FIELDS];
+      const double* p = &h[((size_t)b * c->red_blocks + k) * RED_FIELDS];
       for (int q = 0; q < RED_FIELDS; ++q)
-        if (q != RED_MAX && q != RED_ARG) acc[q] += r[q];
-      if (r[RED_MAX] > best || (r[RED_MAX] == best && r[RED_ARG] < besti)) {
-        best = r[RED_MAX];
-        besti = r[RED_ARG];
+        if (!red_is_max(q)) acc[q] += p[q];
+      acc[RED_PHIMAX] = std::max(acc[RED_PHIMAX], p[RED_PHIMAX]);
+      if (p[RED_MAX] > acc[RED_MAX] || (p[RED_MAX] == acc[RED_MAX] && p[RED_ARG] < acc[RED_ARG])) {
+        acc[RED_MAX] = p[RED_MAX];
+        acc[RED_ARG] = p[RED_ARG];
       }
     }
-    double* o = out + 10 * b;
-    const double m = acc[RED_MASS];
-    o[0] = m * dV;
-    o[1] = best;
-    o[2] = besti;
-    o[3] = m > 0 ? acc[RED_MX] / m : 0.0;
-    o[4] = m > 0 ? acc[RED_MY] / m : 0.0;
-    o[5] = m > 0 ? acc[RED_MZ] / m : 0.0;
-    const double W = -0.5 * acc[RED_W] * dV;
-    const double K = 0.5 * acc[RED_K] * dV;
-    const double Q = 0.5 * acc[RED_Q] * dV;
-    o[6] = W;
-    o[7] = K;
-    o[8] = Q;
-    o[9] = 2 * K + 2 * Q - W;
   }
   return WDM_OK;
+}
+
+// The ten fields of wdm_reduce from one item's RED_* sums.
+static void reduce_fields(const wdm_ctx* c, const std::array<double, RED_FIELDS>& acc, double* o) {
+  const double dV = c->dx * c->dy * c->dz;
+  const double m = acc[RED_MASS];
+  o[0] = m * dV;
+  o[1] = acc[RED_MAX];
+  o[2] = acc[RED_ARG];
+  o[3] = m > 0 ? acc[RED_MX] / m : 0.0;
+  o[4] = m > 0 ? acc[RED_MY] / m : 0.0;
+  o[5] = m > 0 ? acc[RED_MZ] / m : 0.0;
+  const double W = -0.5 * acc[RED_W] * dV;
+  const double K = 0.5 * acc[RED_K] * dV;
+  const double Q = 0.5 * acc[RED_Q] * dV;
+  o[6] = W;
+  o[7] = K;
+  o[8] = Q;
+  o[9] = 2 * K + 2 * Q - W;
+}
+
+wdm_status wdm_reduce(wdm_ctx* c, double* out) {
+  WDM_TRY(need_psi(c));
+  if (!out) return fail(c, WDM_ERR_INVALID, "null output");
+  std::vector<std::array<double, RED_FIELDS>> r;
+  WDM_TRY(reduce_items(c, r));
+  for (int b = 0; b < c->d.batch; ++b) reduce_fields(c, r[(size_t)b], out + 10 * b);
+  return WDM_OK;
+}
+
+// Weighted quantiles over groups of equal values, the groups ascending in
+// value.  Restates the weighted quantile of StatsBase 0.34 (`quantile(v,
+// w::AbstractWeights, p)` for weights other than FrequencyWeights, as
+// src/simulation_main.jl:641 calls it): elements sorted by (value, weight);
+// h = p (sum w - w_1) + w_1; the first element k with cumulative weight S_k > h
+// gives v_{k-1} + (h - S_{k-1}) / (S_k - S_{k-1}) (v_k - v_{k-1}) (v_0 = 0, S_0 = 0);
+// no such element gives the largest value.  Inside a group the first element
+// is its smallest weight: a crossing there interpolates from the previous
+// group's value, a crossing at any later element returns the group's value.
+// Groups of zero total weight are skipped (zero weights take no part).
+// Cumulative sums are FP64.
+static void grouped_quantiles(const double* value, const double* wsum, const double* wmin, int64_t ng, const double* p,
+                              int np, double* out) {
+  std::vector<int64_t> idx;
+  idx.reserve((size_t)ng);
+  for (int64_t g = 0; g < ng; ++g)
+    if (wsum[g] > 0.0) idx.push_back(g);
+  if (idx.empty()) {
+    for (int i = 0; i < np; ++i) out[i] = NAN;
+    return;
+  }
+  std::vector<double> S(idx.size());
+  double acc = 0.0;
+  for (size_t k = 0; k < idx.size(); ++k) S[k] = (acc += wsum[idx[k]]);
+  const double total = acc, w1 = wmin[idx[0]];
+  for (int i = 0; i < np; ++i) {
+    const double h = p[i] * (total - w1) + w1;
+    // first group whose cumulative weight exceeds h
+    const size_t k = (size_t)(std::upper_bound(S.begin(), S.end(), h) - S.begin());
+    if (k >= idx.size()) {
+      out[i] = value[idx.back()];
+      continue;
+    }
+    const double Sprev = k ? S[k - 1] : 0.0, vprev = k ? value[idx[k - 1]] : 0.0;
+    const double m = wmin[idx[k]];
+    const double v = value[idx[k]];
+    out[i] = (h < Sprev + m) ? vprev + (h - Sprev) / m * (v - vprev) : v;
+  }
+}
+
+wdm_status wdm_weighted_quantiles_grouped(const double* value, const double* wsum, const double* wmin, int64_t ngroups,
+                                          const double* p, int32_t np, double* out) {
+  if (ngroups < 0 || np < 0 || (ngroups > 0 && (!value || !wsum || !wmin)) || (np > 0 && (!p || !out)))
+    return fail(nullptr, WDM_ERR_INVALID, "wdm_weighted_quantiles_grouped: bad arguments");
+  for (int64_t g = 1; g < ngroups; ++g)
+    if (!(value[g] > value[g - 1]))
+      return fail(nullptr, WDM_ERR_INVALID, "wdm_weighted_quantiles_grouped: values must ascend strictly");
+  grouped_quantiles(value, wsum, wmin, ngroups, p, np, out);
+  return WDM_OK;
+}
+
+wdm_status wdm_diagnostics(wdm_ctx* c, double* out) {
+  WDM_TRY(need_psi(c));
+  if (!out) return fail(c, WDM_ERR_INVALID, "null output");
+  std::vector<std::array<double, RED_FIELDS>> r;
+  WDM_TRY(reduce_items(c, r));
+  const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
+  // the radii need equal spacings: squared distances are then dx^2 times an integer key
+  const double tol = 1e-12 * c->dx;
+  const bool cubic = std::fabs(c->dx - c->dy) <= tol && std::fabs(c->dx - c->dz) <= tol;
+  const int64_t nkeys = (int64_t)(nx - 1) * (nx - 1) + (int64_t)(ny - 1) * (ny - 1) + (int64_t)(nz - 1) * (nz - 1) + 1;
+  double* wsum = nullptr;
+  unsigned long long* wmin = nullptr;
+  std::vector<double> hs, hm, value;
+  if (cubic) {
+    WDM_CU(c, cudaMalloc((void**)&wsum, sizeof(double) * nkeys));
+    cudaError_t e = cudaMalloc((void**)&wmin, sizeof(unsigned long long) * nkeys);
+    if (e != cudaSuccess) {
+      cudaFree(wsum);
+      return cuda_fail(c, e, "diagnostics histogram");
+    }
+    hs.resize((size_t)nkeys);
+    hm.resize((size_t)nkeys);
+    value.resize((size_t)nkeys);
+    for (int64_t k = 0; k < nkeys; ++k) value[(size_t)k] = c->dx * std::sqrt((double)k);
+  }
+  static const double P[9] = {0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9};
+  wdm_status s = WDM_OK;
+  for (int b = 0; b < c->d.batch && s == WDM_OK; ++b) {
+    const auto& acc = r[(size_t)b];
+    double* o = out + (size_t)WDM_DIAG_FIELDS * b;
+    reduce_fields(c, acc, o);
+    const double dV = c->dx * c->dy * c->dz;
+    o[10] = acc[RED_PX] * dV;
+    o[11] = acc[RED_PY] * dV;
+    o[12] = acc[RED_PZ] * dV;
+    o[13] = acc[RED_PHIMAX];
+    o[14] = std::sqrt(acc[RED_MAX]);
+    o[15] = 2.0 * c->dx * c->dx / M_PI;
+    o[16] = o[13] > 0 ? 2.0 * M_PI / o[13] : INFINITY;
+    o[17] = (c->d.kerr != 0.0 && o[14] > 0) ? 2.0 * M_PI / std::fabs(c->d.kerr) / o[14] : INFINITY;
+    const double sw = acc[RED_SW];
+    if (sw > 0) {
+      const double mean = acc[RED_SWR] / sw;
+      o[18] = std::sqrt(std::max(0.0, acc[RED_SWR2] / sw - mean * mean));
+    } else {
+      o[18] = NAN;
+    }
+    if (!cubic) {
+      for (int i = 0; i < 9; ++i) o[19 + i] = NAN;
+      continue;
+    }
+    const long long arg = (long long)acc[RED_ARG];
+    const int cz = (int)(arg / ((long long)nx * ny)), rem = (int)(arg - (long long)cz * nx * ny);
+    const int cy = rem / nx, cx = rem - cy * nx;
+    cudaError_t e = cudaMemsetAsync(wsum, 0, sizeof(double) * nkeys, c->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(wmin, 0xff, sizeof(unsigned long long) * nkeys, c->st);
+    if (e == cudaSuccess)
+      e = launch_radii_hist(c->psi + (size_t)b * c->ncell, nx, ny, nz, cx, cy, cz, wsum, wmin, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hs.data(), wsum, sizeof(double) * nkeys, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hm.data(), wmin, sizeof(unsigned long long) * nkeys, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+      s = cuda_fail(c, e, "diagnostics histogram");
+      break;
+    }
+    ++c->launch_count;
+    grouped_quantiles(value.data(), hs.data(), hm.data(), nkeys, P, 9, o + 19);
+  }
+  if (wsum) cudaFree(wsum);
+  if (wmin) cudaFree(wmin);
+  return s;
 }
 
 wdm_status wdm_interpolate_phi(wdm_ctx* c, const double* pos, int64_t n, double* out) {

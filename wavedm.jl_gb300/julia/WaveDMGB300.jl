@@ -74,6 +74,19 @@ set_particles!(c::Context, pos::Matrix{Float64}, mass::Vector{Float64}) =  # pos
 step!(c::Context, n, dt; t0=0.0, mode=WDM_STEP_STRANG) =
     check(ccall((:wdm_step, libwavedm), Int32, (Ptr{Cvoid}, Int32, Float64, Float64, Int32), c.h, n, dt, t0, mode), c.h)
 
+const WDM_DIAG_FIELDS = 28
+"""
+The loop diagnostics of SPE3D_waveDM (simulation_main.jl:551-558,641-653) on the
+device, one column per halo: mass, rho_max, argmax (0-based flat index), centre
+of mass, virial sums, momentum, max|Phi|, max|psi|, the compute_timestep limits,
+R, and the radii at p = 0.1:0.1:0.9 about the density maximum (rows 20:28).
+"""
+function diagnostics(c::Context; batch=1)
+    out = zeros(Float64, WDM_DIAG_FIELDS, batch)
+    GC.@preserve out check(ccall((:wdm_diagnostics, libwavedm), Int32, (Ptr{Cvoid}, Ptr{Float64}), c.h, out), c.h)
+    out
+end
+
 # ---------------------------------------------------------------------------
 # drop-in operators of src/solver/KDK.jl for the gpu path (state stays in `c`)
 # ---------------------------------------------------------------------------
