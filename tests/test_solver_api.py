@@ -75,3 +75,52 @@ def test_parallel_poisson_mirror(wdm):
     phi = 4 * np.pi * solver.parallel_poisson([0.5, 0.25, 0.125], [31, 23, 15], rho)
     g = spe.Grid((32, 24, 16), (16.0, 6.0, 2.0))
     assert spe.rel_l2(phi, spe.poisson(rho, g, 4 * np.pi)) < 4e-6
+
+
+def test_prop_csv_has_the_reference_columns(wdm, tmp_path):
+    """save_property_dataframe writes the columns of src/io/save.jl:46-68 in order,
+    lengths scaled by uL, one row per record."""
+    from wavedm_gb300 import solver
+
+    rec = {f: float(i + 1) for i, f in enumerate(wdm.SPEContext.DIAG_FIELDS)}
+    rec["t"] = 0.5
+    path = solver.save_property_dataframe([rec, dict(rec, t=1.0)], str(tmp_path), "T", "S", plot_virial=True, uL=2.0)
+    assert path.endswith("T, S - Prop.csv")
+    lines = open(path).read().splitlines()
+    assert lines[0].split(",") == ["t", "R", "R1", "R2", "R3", "R4", "R5", "R6", "R7", "R8", "R9", "TotalMass",
+                                   "PE_abs", "KE", "QE", "Virial", "MomentumX", "MomentumY", "MomentumZ"]
+    row = [float(v) for v in lines[1].split(",")]
+    assert row[0] == 0.5
+    assert row[1] == 2.0 * rec["R"]
+    assert row[2:11] == [2.0 * rec[f"radius_{k}0"] for k in range(1, 10)]
+    assert row[11] == rec["mass"]
+    assert row[12:] == [rec[k] for k in ("VirialPotential", "TotalKineticE", "TotalQuantumE", "Virial",
+                                         "MomentumX", "MomentumY", "MomentumZ")]
+    assert len(lines) == 3
+    path = solver.save_property_dataframe([rec], str(tmp_path), "T", "S2", plot_virial=False)
+    assert open(path).read().splitlines()[0].split(",")[-1] == "TotalMass"
+
+
+@pytest.mark.gpu
+def test_spe3d_wavedm_writes_prop_files(wdm, tmp_path):
+    """With outputdir the entry writes Prop.csv from the device diagnostics and the
+    final state with psi_last_t one step before the end."""
+    from wavedm_gb300 import solver
+
+    N, X, Nt, Tmax = 32, 6.0, 9, 0.16
+    IC = lambda x, y, z: np.exp(-(x ** 2 + y ** 2 + z ** 2) / 4) * np.exp(0.2j * x)
+    out = solver.SPE3D_waveDM(Nx=N, Xmax=X, Nt=Nt, Tmax=Tmax, IC=IC, StepsBetweenSnapshots=4,
+                              outputdir=str(tmp_path), title="run", suffix="x")
+    lines = open(out["Prop.csv"]).read().splitlines()
+    assert len(lines) == 1 + 2
+    last = dict(zip(lines[0].split(","), map(float, lines[-1].split(","))))
+    assert last["TotalMass"] == pytest.approx(out["Prop"][-1]["mass"], rel=1e-15)
+    assert 0 < last["R1"] < last["R5"] < last["R9"]
+    z = np.load(out["Prop.npz"])
+    assert np.array_equal(z["ψ"], out["psi"])
+    # psi_last_t is the state after Nt - 2 steps of the same dt
+    short = solver.SPE3D_waveDM(Nx=N, Xmax=X, Nt=Nt - 1, Tmax=Tmax * (Nt - 1) / Nt, IC=IC)
+    assert short["dt"] == out["dt"]
+    assert np.allclose(z["ψ_last_t"], short["psi"], rtol=0, atol=1e-6 * np.abs(short["psi"]).max())
+    assert not np.allclose(z["ψ_last_t"], out["psi"], rtol=0, atol=1e-6 * np.abs(out["psi"]).max())
+    assert z["Φ_all"].shape == out["psi"].shape and z["ψ2_averaged"].size == 0

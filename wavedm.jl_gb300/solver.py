@@ -137,7 +137,8 @@ def parallel_poisson(delta, N, rho, boundary="Periodic", backend="gpu"):
 def SPE3D_waveDM(*, Nx=64, Ny=None, Nz=None, Xmax=10.0, Ymax=None, Zmax=None, Nt=100, Tmax=1.0, IC=None, V=None,
                  KDK_flag=True, absorb_coeff=0.0, kappa=0.0, poisson_coeff=4 * np.pi, grid_convention="reference",
                  StepsBetweenSnapshots=None, tidal=None, particles=None, phase_mode="precise", mode=None,
-                 gpu=True, keep_snapshots=False):
+                 gpu=True, keep_snapshots=False, outputdir=None, title="WaveDM", suffix="GB300", plot_virial=True,
+                 uL=1.0):
     """The gpu=true solver entry of SPE3D_waveDM with its keyword arguments for the path.
 
     IC: callable IC(x, y, z) -> complex (broadcast over the grid) or an array
@@ -146,7 +147,14 @@ def SPE3D_waveDM(*, Nx=64, Ny=None, Nz=None, Xmax=10.0, Ymax=None, Zmax=None, Nt
     simulation_main.jl:538) or "lie" (KDK_flag false).  tidal: callable t ->
     (Txx, Tyy, Tzz, Txy, Txz, Tyz) for the 1/2 x^T T x tide.  particles:
     (pos [n,3], mass [n]) CIC-deposited each step.  Returns a dict with psi, t,
-    dt and per-snapshot diagnostics (mass, rho_max, centre of mass, virial sums).
+    dt and the per-snapshot diagnostics of the reference loop (wdm_diagnostics:
+    mass, density maximum and its index, the radii R1..R9 about it, R, virial
+    and momentum sums, timestep limits).  With outputdir, writes the
+    reference's "<title>, <suffix> - Prop.csv" (save_property_dataframe,
+    src/io/save.jl:41-72) and the final state "<title>, <suffix> - Prop.npz"
+    with the keys of save_evolution_results (src/io/save.jl:25-34); the .npz
+    stands in for JLD2, which needs an HDF5 library (the Julia module writes
+    the .jld2 itself).
     """
     if not gpu:
         raise ValueError("this library is the gpu=true path; there is no CPU fallback")
@@ -181,13 +189,24 @@ def SPE3D_waveDM(*, Nx=64, Ny=None, Nz=None, Xmax=10.0, Ymax=None, Zmax=None, Nt
         records, snaps = [], []
         done = 0
         total = Nt - 1
+        psi_last_t = None
         while done < total:
             n = min(stride, total - done)
             if tidal is not None:
                 ctx.set_tidal([tidal(t0) for t0 in (done + np.arange(n + 1)) * dt])
-            ctx.step(n, dt, t0=done * dt, mode=mode)
+            if outputdir is not None and done + n == total and n > 1:
+                # the state one step before the end (psi_last_t of the reference loop)
+                ctx.step(n - 1, dt, t0=done * dt, mode=mode)
+                psi_last_t = ctx.get_psi()
+                if tidal is not None:
+                    ctx.set_tidal([tidal(t0) for t0 in (done + n - 1 + np.arange(2)) * dt])
+                ctx.step(1, dt, t0=(done + n - 1) * dt, mode=mode)
+            else:
+                if outputdir is not None and done + n == total:
+                    psi_last_t = ctx.get_psi()
+                ctx.step(n, dt, t0=done * dt, mode=mode)
             done += n
-            rec = ctx.reduce()
+            rec = ctx.diagnostics()
             rec["t"] = done * dt
             records.append(rec)
             if keep_snapshots:
@@ -195,6 +214,51 @@ def SPE3D_waveDM(*, Nx=64, Ny=None, Nz=None, Xmax=10.0, Ymax=None, Zmax=None, Nt
         out = {"psi": ctx.get_psi(), "t": t, "dt": dt, "Nt": Nt, "Prop": records}
         if keep_snapshots:
             out["snapshots"] = snaps
+        if outputdir is not None:
+            out["Prop.csv"] = save_property_dataframe(records, outputdir, title, suffix, plot_virial=plot_virial, uL=uL)
+            out["Prop.npz"] = save_evolution_results(out["psi"], ctx.get_phi(), psi_last_t, None, outputdir, title,
+                                                     suffix)
         return out
     finally:
         ctx.close()
+
+
+PROP_COLUMNS = ("t", "R", "R1", "R2", "R3", "R4", "R5", "R6", "R7", "R8", "R9", "TotalMass")
+PROP_VIRIAL_COLUMNS = ("PE_abs", "KE", "QE", "Virial", "MomentumX", "MomentumY", "MomentumZ")
+
+
+def save_property_dataframe(records, outputdir, title, suffix, plot_virial=True, uL=1.0):
+    """Write "<title>, <suffix> - Prop.csv" as src/io/save.jl:41-72 does: one row
+    per record of SPEContext.diagnostics() (plus its "t"), columns t, R,
+    R1..R9 (lengths times uL, as the loop stores them), TotalMass and, with
+    plot_virial, PE_abs KE QE Virial MomentumX..Z.  Returns the path."""
+    import csv
+    import os
+
+    cols = PROP_COLUMNS + (PROP_VIRIAL_COLUMNS if plot_virial else ())
+    path = os.path.join(outputdir, f"{title}, {suffix} - Prop.csv")
+    with open(path, "w", newline="") as f:
+        w = csv.writer(f)
+        w.writerow(cols)
+        for r in records:
+            row = [r["t"], r["R"] * uL] + [r[f"radius_{k}0"] * uL for k in range(1, 10)] + [r["mass"]]
+            if plot_virial:
+                row += [r["VirialPotential"], r["TotalKineticE"], r["TotalQuantumE"], r["Virial"],
+                        r["MomentumX"], r["MomentumY"], r["MomentumZ"]]
+            w.writerow([repr(float(v)) for v in row])
+    return path
+
+
+def save_evolution_results(psi, phi_all, psi_last_t, averaged_psi2, outputdir, title, suffix):
+    """The final state with the keys of src/io/save.jl:25-34 ("ψ", "Φ_all",
+    "ψ_last_t", "ψ2_averaged"), as "<title>, <suffix> - Prop.npz" (arrays in the
+    library's [nz][ny][nx] order; an absent array is stored as an empty one).
+    Returns the path."""
+    import os
+
+    path = os.path.join(outputdir, f"{title}, {suffix} - Prop.npz")
+    empty = np.zeros(0)
+    np.savez(path, **{"ψ": psi, "Φ_all": phi_all,
+                      "ψ_last_t": psi_last_t if psi_last_t is not None else empty,
+                      "ψ2_averaged": averaged_psi2 if averaged_psi2 is not None else empty})
+    return path
