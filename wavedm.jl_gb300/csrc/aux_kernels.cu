@@ -92,7 +92,23 @@ cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t
 // One block partial per (block, batch item): RED_FIELDS doubles.  The sums
 // restate src/visualization/runtime.jl:210-238 (interior cells, second-order
 // central differences) and src/simulation_main.jl:652 (total mass).
-constexpr int RED_THREADS = 256;
+constexpr int RED_THREADS = 128;
+
+// Per-thread running sum as an unevaluated float pair hi + lo (Knuth's
+// two-sum moves every rounding error of hi into lo).  A thread adds a few
+// hundred terms, so hi + lo carries the sum to about 2^-44 relative: FP64
+// accuracy for the totals without FP64 arithmetic per cell, which this GPU
+// runs at a small fraction of its FP32 rate.
+struct FAcc {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float s = hi + v;
+    const float bb = s - hi;
+    lo += (hi - (s - bb)) + (v - bb);
+    hi = s;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 __global__ void __launch_bounds__(RED_THREADS)
 k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, RedGeom g,
@@ -101,43 +117,50 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
   const long long n = nxy * g.nz;
   const float2* psi = psi_all + blockIdx.y * n;
   const float* phi = phi_all + blockIdx.y * n;
-  double acc[RED_FIELDS];
-#pragma unroll
-  for (int q = 0; q < RED_FIELDS; ++q) acc[q] = 0.0;
-  acc[RED_MAX] = -1.0;
-  acc[RED_ARG] = 0.0;
-  acc[RED_PHIMAX] = 0.0;
+  FAcc mass, mx, my, mz, wp, kk, q, px, py, pz;
+  float best_hi = -1.f, best_lo = 0.f, phimax = 0.f;
+  long long best_i = 0;
+  double sw = 0.0, swr = 0.0, swr2 = 0.0;  // one z-slice only: FP64 is cheap there
   const float fi2dx = (float)(0.5 / g.dx), fi2dy = (float)(0.5 / g.dy), fi2dz = (float)(0.5 / g.dz);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int z = (int)(i / nxy);
-    const long long rem = i - z * nxy;
-    const int y = (int)(rem / g.nx);
-    const int x = (int)(rem - (long long)y * g.nx);
+  const float fx0 = (float)g.x0, fy0 = (float)g.y0, fz0 = (float)g.z0;
+  const float fdx = (float)g.dx, fdy = (float)g.dy, fdz = (float)g.dz;
+  // rows (y, z) over the blocks, x over the threads: one index division per row
+  const long long nrows = (long long)g.ny * g.nz;
+  for (long long row = blockIdx.x; row < nrows; row += gridDim.x)
+  for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
+    const int z = (int)(row / g.ny);
+    const int y = (int)(row - (long long)z * g.ny);
+    const long long i = row * g.nx + x;
     const float2 p = psi[i];
-    const double rho = (double)p.x * p.x + (double)p.y * p.y;
-    acc[RED_MASS] += rho;
-    acc[RED_MX] += rho * (g.x0 + g.dx * x);
-    acc[RED_MY] += rho * (g.y0 + g.dy * y);
-    acc[RED_MZ] += rho * (g.z0 + g.dz * z);
-    if (rho > acc[RED_MAX]) {
-      acc[RED_MAX] = rho;
-      acc[RED_ARG] = (double)i;
+    // rho = p.x^2 + p.y^2 exactly as (rs, rt): two-product of each square, two-sum of the pair
+    const float a = p.x * p.x, b = p.y * p.y;
+    const float ea = fmaf(p.x, p.x, -a), eb = fmaf(p.y, p.y, -b);
+    const float rs = a + b;
+    const float bb = rs - a;
+    const float rt = ((a - (rs - bb)) + (b - bb)) + (ea + eb);
+    mass.add(rs);
+    mass.lo += rt;
+    mx.add(rs * fmaf(fdx, (float)x, fx0));
+    my.add(rs * fmaf(fdy, (float)y, fy0));
+    mz.add(rs * fmaf(fdz, (float)z, fz0));
+    if (rs > best_hi || (rs == best_hi && rt > best_lo)) {
+      best_hi = rs;
+      best_lo = rt;
+      best_i = i;
     }
-    const double ph = (double)phi[i];
-    acc[RED_PHIMAX] = fmax(acc[RED_PHIMAX], fabs(ph));
+    const float ph = phi[i];
+    phimax = fmaxf(phimax, fabsf(ph));
     if (z == g.zmid) {
+      const double rho = (double)rs + (double)rt;
       const double fx = g.x0 + g.dx * x, fy = g.y0 + g.dy * y, fz = g.z0 + g.dz * z;
       const double r2 = fx * fx + fy * fy + fz * fz;
-      acc[RED_SW] += rho;
-      acc[RED_SWR] += rho * sqrt(r2);
-      acc[RED_SWR2] += rho * r2;
+      sw += rho;
+      swr += rho * sqrt(r2);
+      swr2 += rho * r2;
     }
     if (x > 0 && x < g.nx - 1 && y > 0 && y < g.ny - 1 && z > 0 && z < g.nz - 1) {
-      // Per-cell terms in FP32 (the reference forms them from its FP32 psi
-      // too); every sum accumulates in FP64.  FP64 arithmetic per cell (six
-      // square roots) made this kernel compute-bound on this GPU's FP64 units.
-      const float rf = fmaf(p.x, p.x, p.y * p.y);
-      acc[RED_W] += (double)(rf * phi[i]);
+      // per-cell terms in FP32 (the reference forms them from its FP32 psi too)
+      wp.add(rs * ph);
       const float2 xp = psi[i + 1], xm = psi[i - 1];
       const float2 yp = psi[i + g.nx], ym = psi[i - g.nx];
       const float2 zp = psi[i + nxy], zm = psi[i - nxy];
@@ -148,17 +171,34 @@ k_reduce(const float2* __restrict__ psi_all, const float* __restrict__ phi_all, 
       const float jx = fmaf(p.x, gxi, -p.y * gxr);
       const float jy = fmaf(p.x, gyi, -p.y * gyr);
       const float jz = fmaf(p.x, gzi, -p.y * gzr);
-      acc[RED_PX] += (double)jx;
-      acc[RED_PY] += (double)jy;
-      acc[RED_PZ] += (double)jz;
-      if (rf > 0.f) acc[RED_K] += (double)(fmaf(jx, jx, fmaf(jy, jy, jz * jz)) / rf);
+      px.add(jx);
+      py.add(jy);
+      pz.add(jz);
+      if (rs > 0.f) kk.add(fmaf(jx, jx, fmaf(jy, jy, jz * jz)) / rs);
       auto mag = [](float2 v) { return sqrtf(fmaf(v.x, v.x, v.y * v.y)); };
       const float ax = (mag(xp) - mag(xm)) * fi2dx;
       const float ay = (mag(yp) - mag(ym)) * fi2dy;
       const float az = (mag(zp) - mag(zm)) * fi2dz;
-      acc[RED_Q] += (double)fmaf(ax, ax, fmaf(ay, ay, az * az));
+      q.add(fmaf(ax, ax, fmaf(ay, ay, az * az)));
     }
   }
+  double acc[RED_FIELDS];
+  acc[RED_MASS] = mass.value();
+  acc[RED_MAX] = best_hi < 0.f ? -1.0 : (double)best_hi + (double)best_lo;
+  acc[RED_ARG] = (double)best_i;
+  acc[RED_MX] = mx.value();
+  acc[RED_MY] = my.value();
+  acc[RED_MZ] = mz.value();
+  acc[RED_W] = wp.value();
+  acc[RED_K] = kk.value();
+  acc[RED_Q] = q.value();
+  acc[RED_PX] = px.value();
+  acc[RED_PY] = py.value();
+  acc[RED_PZ] = pz.value();
+  acc[RED_PHIMAX] = (double)phimax;
+  acc[RED_SW] = sw;
+  acc[RED_SWR] = swr;
+  acc[RED_SWR2] = swr2;
   // block reduction (warp shuffles, then one warp over the warp results)
   __shared__ double sh[RED_THREADS / 32][RED_FIELDS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -207,32 +247,73 @@ cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g,
 }
 
 // Weights of the distances from the density maximum (the weighted quantiles of
-// src/simulation_main.jl:641-650), keyed by the squared distance in cells.
-// Cells of zero density take no part, as zero weights take none in the
-// weighted quantile.
-__global__ void k_radii_hist(const float2* __restrict__ psi, int nx, int ny, int nz, int cx, int cy, int cz,
-                             double* __restrict__ wsum, unsigned long long* __restrict__ wmin) {
-  const long long nxy = (long long)nx * ny, n = nxy * nz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const float2 p = psi[i];
-    const double rho = (double)p.x * p.x + (double)p.y * p.y;
-    if (!(rho > 0.0)) continue;
-    const int z = (int)(i / nxy);
-    const long long rem = i - z * nxy;
-    const int y = (int)(rem / nx);
-    const int x = (int)(rem - (long long)y * nx);
-    const long long ddx = x - cx, ddy = y - cy, ddz = z - cz;
-    const long long key = ddx * ddx + ddy * ddy + ddz * ddz;
-    atomicAdd(&wsum[key], rho);
-    atomicMin(&wmin[key], (unsigned long long)__double_as_longlong(rho));
+// src/simulation_main.jl:641-650), keyed by the squared distance in cells.  A
+// thread takes one offset (a, b, c) >= 0 and sums the up to eight cells at
+// (cx +- a, cy +- b, cz +- c) inside the grid, which share the key
+// a^2 + b^2 + c^2, so a centred halo needs one atomic add per eight cells.
+__global__ void k_radii_hist(const float2* __restrict__ psi, int nx, int ny, int nz, int cx, int cy, int cz, int da,
+                             int db, int dc, double* __restrict__ wsum) {
+  const int nbc = db * dc;
+  for (int bc = blockIdx.x; bc < nbc; bc += gridDim.x)
+  for (int a = threadIdx.x; a < da; a += blockDim.x) {
+    const int c = bc / db;
+    const int b = bc - c * db;
+    double s = 0.0;
+    for (int sz = 0; sz < (c ? 2 : 1); ++sz) {
+      const int zz = sz ? cz - c : cz + c;
+      if (zz < 0 || zz >= nz) continue;
+      for (int sy = 0; sy < (b ? 2 : 1); ++sy) {
+        const int yy = sy ? cy - b : cy + b;
+        if (yy < 0 || yy >= ny) continue;
+        const long long row = ((long long)zz * ny + yy) * nx;
+        for (int sx = 0; sx < (a ? 2 : 1); ++sx) {
+          const int xx = sx ? cx - a : cx + a;
+          if (xx < 0 || xx >= nx) continue;
+          const float2 p = psi[row + xx];
+          s += (double)p.x * p.x + (double)p.y * p.y;
+        }
+      }
+    }
+    if (s > 0.0) atomicAdd(&wsum[(long long)a * a + (long long)b * b + (long long)c * c], s);
   }
 }
 
 cudaError_t launch_radii_hist(const float2* psi, int nx, int ny, int nz, int cx, int cy, int cz, double* wsum,
-                              unsigned long long* wmin, cudaStream_t st) {
-  const long long n = (long long)nx * ny * nz;
-  const long long b = (n + 255) / 256;
-  k_radii_hist<<<(unsigned)(b < 152 * 16 ? b : 152 * 16), 256, 0, st>>>(psi, nx, ny, nz, cx, cy, cz, wsum, wmin);
+                              cudaStream_t st) {
+  const int da = (cx > nx - 1 - cx ? cx : nx - 1 - cx) + 1;
+  const int db = (cy > ny - 1 - cy ? cy : ny - 1 - cy) + 1;
+  const int dc = (cz > nz - 1 - cz ? cz : nz - 1 - cz) + 1;
+  const int rows = db * dc;
+  k_radii_hist<<<(unsigned)(rows < 152 * 32 ? rows : 152 * 32), 128, 0, st>>>(psi, nx, ny, nz, cx, cy, cz, da, db, dc,
+                                                                              wsum);
+  return cudaGetLastError();
+}
+
+// Smallest nonzero weight (bits of a positive double) among the cells whose
+// key is one of keys.k[0..n): the few groups the quantiles fall in.
+__global__ void k_radii_min(const float2* __restrict__ psi, int nx, int ny, int nz, int cx, int cy, int cz,
+                            RadiiKeys keys, unsigned long long* __restrict__ wmin) {
+  const int nrows = ny * nz;
+  for (int row = blockIdx.x; row < nrows; row += gridDim.x)
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+    const int z = row / ny;
+    const int y = row - z * ny;
+    const long long i = (long long)row * nx + x;
+    const long long ddx = x - cx, ddy = y - cy, ddz = z - cz;
+    const long long key = ddx * ddx + ddy * ddy + ddz * ddz;
+    for (int j = 0; j < keys.n; ++j)
+      if (key == keys.k[j]) {
+        const float2 p = psi[i];
+        const double rho = (double)p.x * p.x + (double)p.y * p.y;
+        if (rho > 0.0) atomicMin(&wmin[j], (unsigned long long)__double_as_longlong(rho));
+      }
+  }
+}
+
+cudaError_t launch_radii_min(const float2* psi, int nx, int ny, int nz, int cx, int cy, int cz, const RadiiKeys& keys,
+                             unsigned long long* wmin, cudaStream_t st) {
+  const int rows = ny * nz;
+  k_radii_min<<<(unsigned)(rows < 152 * 32 ? rows : 152 * 32), 128, 0, st>>>(psi, nx, ny, nz, cx, cy, cz, keys, wmin);
   return cudaGetLastError();
 }
 

@@ -42,10 +42,18 @@ struct RedGeom {
 };
 
 // Lagrangian radii: per squared cell distance key = di^2 + dj^2 + dk^2 from
-// cell (cx, cy, cz), the FP64 sum of rho and the smallest nonzero rho (as the
-// bits of a positive double) over the cells at that distance.
+// cell (cx, cy, cz), the FP64 sum of rho over the cells at that distance;
+// then, for up to RADII_KEYS keys, the smallest nonzero rho (as the bits of a
+// positive double) over their cells.
+constexpr int RADII_KEYS = 16;
+struct RadiiKeys {
+  long long k[RADII_KEYS];
+  int n;
+};
 cudaError_t launch_radii_hist(const float2* psi, int nx, int ny, int nz, int cx, int cy, int cz, double* wsum,
-                              unsigned long long* wmin, cudaStream_t st);
+                              cudaStream_t st);
+cudaError_t launch_radii_min(const float2* psi, int nx, int ny, int nz, int cx, int cy, int cz, const RadiiKeys& keys,
+                             unsigned long long* wmin, cudaStream_t st);
 
 cudaError_t launch_abs2(const float2* psi, float* out, long long n, cudaStream_t st);
 // Adjoint seed of L = sum (|psi|^2 - rho_t)^2 dV: lam = 4 (|psi|^2 - rho_t) psi dV,

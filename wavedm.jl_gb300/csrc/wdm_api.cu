@@ -1189,34 +1189,47 @@ wdm_status wdm_reduce(wdm_ctx* c, double* out) {
 // group's value, a crossing at any later element returns the group's value.
 // Groups of zero total weight are skipped (zero weights take no part).
 // Cumulative sums are FP64.
-static void grouped_quantiles(const double* value, const double* wsum, const double* wmin, int64_t ng, const double* p,
-                              int np, double* out) {
-  std::vector<int64_t> idx;
-  idx.reserve((size_t)ng);
-  for (int64_t g = 0; g < ng; ++g)
-    if (wsum[g] > 0.0) idx.push_back(g);
-  if (idx.empty()) {
+struct GroupCum {
+  std::vector<int64_t> idx;  // nonempty groups, ascending
+  std::vector<double> S;     // cumulative weight through each
+  explicit GroupCum(const double* wsum, int64_t ng) {
+    double acc = 0.0;
+    for (int64_t g = 0; g < ng; ++g)
+      if (wsum[g] > 0.0) {
+        idx.push_back(g);
+        S.push_back(acc += wsum[g]);
+      }
+  }
+  // position in idx of the first group whose cumulative weight exceeds h (idx.size(): none)
+  size_t find(double h) const { return (size_t)(std::upper_bound(S.begin(), S.end(), h) - S.begin()); }
+  double h(double p, double w1) const { return p * (S.back() - w1) + w1; }
+};
+
+// value(g) and wmin(g): a group's value and smallest element weight; only
+// the first group, the groups the quantiles fall in and their predecessors
+// are asked for.
+extern "C++" {
+template <class Value, class Wmin>
+static void grouped_quantiles(const GroupCum& gc, Value value, Wmin wmin, const double* p, int np, double* out) {
+  if (gc.idx.empty()) {
     for (int i = 0; i < np; ++i) out[i] = NAN;
     return;
   }
-  std::vector<double> S(idx.size());
-  double acc = 0.0;
-  for (size_t k = 0; k < idx.size(); ++k) S[k] = (acc += wsum[idx[k]]);
-  const double total = acc, w1 = wmin[idx[0]];
+  const double w1 = wmin(gc.idx[0]);
   for (int i = 0; i < np; ++i) {
-    const double h = p[i] * (total - w1) + w1;
-    // first group whose cumulative weight exceeds h
-    const size_t k = (size_t)(std::upper_bound(S.begin(), S.end(), h) - S.begin());
-    if (k >= idx.size()) {
-      out[i] = value[idx.back()];
+    const double h = gc.h(p[i], w1);
+    const size_t k = gc.find(h);
+    if (k >= gc.idx.size()) {
+      out[i] = value(gc.idx.back());
       continue;
     }
-    const double Sprev = k ? S[k - 1] : 0.0, vprev = k ? value[idx[k - 1]] : 0.0;
-    const double m = wmin[idx[k]];
-    const double v = value[idx[k]];
+    const double Sprev = k ? gc.S[k - 1] : 0.0, vprev = k ? value(gc.idx[k - 1]) : 0.0;
+    const double m = wmin(gc.idx[k]);
+    const double v = value(gc.idx[k]);
     out[i] = (h < Sprev + m) ? vprev + (h - Sprev) / m * (v - vprev) : v;
   }
 }
+}  // extern "C++"
 
 wdm_status wdm_weighted_quantiles_grouped(const double* value, const double* wsum, const double* wmin, int64_t ngroups,
                                           const double* p, int32_t np, double* out) {
@@ -1225,7 +1238,9 @@ wdm_status wdm_weighted_quantiles_grouped(const double* value, const double* wsu
   for (int64_t g = 1; g < ngroups; ++g)
     if (!(value[g] > value[g - 1]))
       return fail(nullptr, WDM_ERR_INVALID, "wdm_weighted_quantiles_grouped: values must ascend strictly");
-  grouped_quantiles(value, wsum, wmin, ngroups, p, np, out);
+  const GroupCum gc(wsum, ngroups);
+  grouped_quantiles(
+      gc, [&](int64_t g) { return value[g]; }, [&](int64_t g) { return wmin[g]; }, p, np, out);
   return WDM_OK;
 }
 
@@ -1241,18 +1256,15 @@ wdm_status wdm_diagnostics(wdm_ctx* c, double* out) {
   const int64_t nkeys = (int64_t)(nx - 1) * (nx - 1) + (int64_t)(ny - 1) * (ny - 1) + (int64_t)(nz - 1) * (nz - 1) + 1;
   double* wsum = nullptr;
   unsigned long long* wmin = nullptr;
-  std::vector<double> hs, hm, value;
+  std::vector<double> hs;
   if (cubic) {
     WDM_CU(c, cudaMalloc((void**)&wsum, sizeof(double) * nkeys));
-    cudaError_t e = cudaMalloc((void**)&wmin, sizeof(unsigned long long) * nkeys);
+    cudaError_t e = cudaMalloc((void**)&wmin, sizeof(unsigned long long) * RADII_KEYS);
     if (e != cudaSuccess) {
       cudaFree(wsum);
       return cuda_fail(c, e, "diagnostics histogram");
     }
     hs.resize((size_t)nkeys);
-    hm.resize((size_t)nkeys);
-    value.resize((size_t)nkeys);
-    for (int64_t k = 0; k < nkeys; ++k) value[(size_t)k] = c->dx * std::sqrt((double)k);
   }
   static const double P[9] = {0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9};
   wdm_status s = WDM_OK;
@@ -1283,21 +1295,46 @@ wdm_status wdm_diagnostics(wdm_ctx* c, double* out) {
     const long long arg = (long long)acc[RED_ARG];
     const int cz = (int)(arg / ((long long)nx * ny)), rem = (int)(arg - (long long)cz * nx * ny);
     const int cy = rem / nx, cx = rem - cy * nx;
+    // pass 1: the weight of every distance
     cudaError_t e = cudaMemsetAsync(wsum, 0, sizeof(double) * nkeys, c->st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(wmin, 0xff, sizeof(unsigned long long) * nkeys, c->st);
-    if (e == cudaSuccess)
-      e = launch_radii_hist(c->psi + (size_t)b * c->ncell, nx, ny, nz, cx, cy, cz, wsum, wmin, c->st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(hs.data(), wsum, sizeof(double) * nkeys, cudaMemcpyDeviceToHost, c->st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(hm.data(), wmin, sizeof(unsigned long long) * nkeys, cudaMemcpyDeviceToHost, c->st);
+    const float2* pb = c->psi + (size_t)b * c->ncell;
+    if (e == cudaSuccess) e = launch_radii_hist(pb, nx, ny, nz, cx, cy, cz, wsum, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hs.data(), wsum, sizeof(double) * nkeys, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    // pass 2: the smallest element weight of the distance 0 (w_1) and of the
+    // groups the quantiles fall in, the only ones the quantile reads
+    RadiiKeys keys{};
+    keys.k[keys.n++] = 0;
+    const GroupCum gc(hs.data(), e == cudaSuccess ? nkeys : 0);
+    if (!gc.idx.empty())
+      for (int i = 0; i < 9; ++i) {
+        const size_t k = gc.find(gc.h(P[i], acc[RED_MAX]));  // w_1 is the maximum's weight
+        if (k >= gc.idx.size()) continue;
+        const long long key = gc.idx[k];
+        if (std::find(keys.k, keys.k + keys.n, key) == keys.k + keys.n && keys.n < RADII_KEYS) keys.k[keys.n++] = key;
+      }
+    unsigned long long m[RADII_KEYS];
+    if (e == cudaSuccess) e = cudaMemsetAsync(wmin, 0xff, sizeof(unsigned long long) * RADII_KEYS, c->st);
+    if (e == cudaSuccess) e = launch_radii_min(pb, nx, ny, nz, cx, cy, cz, keys, wmin, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m, wmin, sizeof(m), cudaMemcpyDeviceToHost, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     if (e != cudaSuccess) {
       s = cuda_fail(c, e, "diagnostics histogram");
       break;
     }
-    ++c->launch_count;
-    grouped_quantiles(value.data(), hs.data(), hm.data(), nkeys, P, 9, o + 19);
+    c->launch_count += 2;
+    const double dx = c->dx;
+    auto value = [dx](int64_t g) { return dx * std::sqrt((double)g); };
+    auto wmin_of = [&](int64_t g) {
+      for (int j = 0; j < keys.n; ++j)
+        if (keys.k[j] == g) {
+          double v;
+          std::memcpy(&v, &m[j], sizeof(v));
+          return v;
+        }
+      return (double)INFINITY;  // not a group the quantiles fall in
+    };
+    grouped_quantiles(gc, value, wmin_of, P, 9, o + 19);
   }
   if (wsum) cudaFree(wsum);
   if (wmin) cudaFree(wmin);
