@@ -228,6 +228,24 @@ def run_native(args, rank, world):
         nb = psi0.nbytes
         e2e = {"value": ne * world / el, "unit": "steps/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ne, "calls_per_step": ["wdm_set_psi(host)", "wdm_step(1)", "wdm_get_psi(host)"]}
+    # The reference loop with its per-step diagnostics: K(dt/2) D(dt) per
+    # iteration (src/simulation_main.jl:538-547), then findmax, the radii
+    # quantiles, R and the mass (:551-558, :641-653), here on the device.
+    loop = None
+    if not args.no_e2e:
+        nl = max(1, min(K, args.e2e_steps))
+        ctx.set_psi(psi0)
+        for _ in range(2):
+            ctx.step(1, dt, mode="reference_loop")
+            ctx.diagnostics()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(nl):
+            ctx.step(1, dt, mode="reference_loop")
+            ctx.diagnostics()
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        loop = {"value": nl * world / el, "unit": "steps/s", "steps": nl,
+                "calls_per_step": ["wdm_step(1, reference_loop)", "wdm_diagnostics"]}
     sched = ctx.line_schedule()
     ctx.close()
 
@@ -270,6 +288,7 @@ def run_native(args, rank, world):
         "line_schedule": sched,
         "gpu_launches": int(launches),
         "e2e": e2e,
+        "loop_with_diagnostics": loop,
         "clocks": clk,
     }
     return rec
@@ -424,6 +443,25 @@ def time_oracle(wl, budget_s, max_steps, warm=1):
             break
     el = time.perf_counter() - t0
     return n / el, n, spe.WORKERS
+
+
+def time_oracle_loop(wl, budget_s):
+    """The reference loop on the host cores: one literal K(dt/2) D(dt) iteration of
+    the FP64 oracle plus the loop's per-step diagnostics (the potential, findmax,
+    the weighted radii quantiles, R, mass), until the budget is spent."""
+    spe, g, phys = oracle_setup(wl, 4)
+    dt = wl["dt"]
+    psi = wl["psi0"].astype(np.complex64).astype(np.complex128)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        psi = spe.kdk_step(psi, g, phys, n * dt, dt, mode="reference_loop")
+        spe.loop_diagnostics(psi, spe.potential(psi, g, phys, (n + 1) * dt), g)
+        spe.mass(psi, g)
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 3:
+            break
+    return n / (time.perf_counter() - t0), n, spe.WORKERS
 
 
 def run_adjoint(args, rank, world):
@@ -588,6 +626,13 @@ def main():
         v, n, cores = time_oracle(wl, budget_s=args.cpu_budget, max_steps=1000, warm=1)
         rec["cpu_baseline"] = {"value": round(v, 5), "unit": "steps/s", "cores": cores, "kind": "port",
                                "sample": f"{n} FP64 Strang steps of the full {wl['n']}^3 workload (1 warm-up)"}
+        if not args.no_e2e:
+            v, n, cores = time_oracle_loop(wl, budget_s=args.cpu_budget)
+            rec["cpu_baseline_loop"] = {
+                "value": round(v, 5), "unit": "steps/s", "cores": cores, "kind": "port",
+                "sample": f"{n} FP64 reference-loop iterations of the full {wl['n']}^3 workload, each with the "
+                          "loop's host diagnostics (potential, findmax, radii quantiles, R, mass)",
+                "compare_with": "loop_with_diagnostics"}
     if world > 1:
         import torch
 

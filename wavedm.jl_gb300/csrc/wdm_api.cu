@@ -158,6 +158,9 @@ struct wdm_ctx {
   std::vector<float2*> slot2_psi, slot2_H;              // segment states, set 1
   cudaStream_t st_rec = nullptr;    // adjoint: recompute of the next segment, beside the reverse sweep
   cudaEvent_t ev_ck = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_bwd[2] = {nullptr, nullptr};
+  // diagnostics: radii histogram and minimum words (allocated on first use)
+  double* diag_wsum = nullptr;
+  unsigned long long* diag_wmin = nullptr;
   long long version = 0;            // bumped by every set_* call that a captured graph bakes in
   struct wdm_group* self_group = nullptr;  // single-member group of wdm_step_graph
   Profiler prof;
@@ -629,7 +632,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
     if (p) cudaFree(p);
-  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc};
+  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc, c->diag_wsum, c->diag_wmin};
   for (void* p : adj)
     if (p) cudaFree(p);
   for (auto* v : {&c->ck_psi, &c->ck_H, &c->slot_psi, &c->slot_H, &c->slot2_psi, &c->slot2_H})
@@ -1254,18 +1257,15 @@ wdm_status wdm_diagnostics(wdm_ctx* c, double* out) {
   const double tol = 1e-12 * c->dx;
   const bool cubic = std::fabs(c->dx - c->dy) <= tol && std::fabs(c->dx - c->dz) <= tol;
   const int64_t nkeys = (int64_t)(nx - 1) * (nx - 1) + (int64_t)(ny - 1) * (ny - 1) + (int64_t)(nz - 1) * (nz - 1) + 1;
-  double* wsum = nullptr;
-  unsigned long long* wmin = nullptr;
   std::vector<double> hs;
   if (cubic) {
-    WDM_CU(c, cudaMalloc((void**)&wsum, sizeof(double) * nkeys));
-    cudaError_t e = cudaMalloc((void**)&wmin, sizeof(unsigned long long) * RADII_KEYS);
-    if (e != cudaSuccess) {
-      cudaFree(wsum);
-      return cuda_fail(c, e, "diagnostics histogram");
-    }
+    // the histogram (nkeys doubles) and the minimum words live with the context
+    if (!c->diag_wsum) WDM_TRY(dalloc(c, &c->diag_wsum, (size_t)nkeys));
+    if (!c->diag_wmin) WDM_TRY(dalloc(c, &c->diag_wmin, (size_t)RADII_KEYS));
     hs.resize((size_t)nkeys);
   }
+  double* wsum = c->diag_wsum;
+  unsigned long long* wmin = c->diag_wmin;
   static const double P[9] = {0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9};
   wdm_status s = WDM_OK;
   for (int b = 0; b < c->d.batch && s == WDM_OK; ++b) {
@@ -1336,8 +1336,6 @@ wdm_status wdm_diagnostics(wdm_ctx* c, double* out) {
     };
     grouped_quantiles(gc, value, wmin_of, P, 9, o + 19);
   }
-  if (wsum) cudaFree(wsum);
-  if (wmin) cudaFree(wmin);
   return s;
 }
 
