@@ -340,19 +340,6 @@ __global__ void k_cic_deposit(float* __restrict__ rho, const CicParticle* __rest
   }
 }
 
-__global__ void k_cic_clear(float* __restrict__ rho, const CicParticle* __restrict__ p, long long n, int nx, int ny,
-                            int nz, int* __restrict__ rows) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const CicParticle a = p[q];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const long long cell = cic_cell(a.i[0] + (c & 1), a.i[1] + ((c >> 1) & 1), a.i[2] + (c >> 2), nx, ny, nz);
-    rho[cell] = 0.f;
-    if (rows && c % 2 == 0) rows[cell / nx] = 0;
-  }
-}
-
 __global__ void k_cic_interp(const float* __restrict__ f, const CicParticle* __restrict__ p, long long n, int nx,
                              int ny, int nz, double* __restrict__ out) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -372,13 +359,6 @@ cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, in
                                cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   k_cic_deposit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz, rows);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_cic_clear(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, int* rows,
-                             cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  k_cic_clear<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rho, p, n, nx, ny, nz, rows);
   return cudaGetLastError();
 }
 

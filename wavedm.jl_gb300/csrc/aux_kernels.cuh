@@ -69,13 +69,11 @@ cudaError_t launch_mean_shift(const void* data, bool complex_in, long long n, in
                               double add, cudaStream_t st);
 cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g, double* partials, int nblocks,
                           int batch, cudaStream_t st);
-// CIC deposit of the particles into rho (cleared afterwards by launch_cic_clear,
-// which zeroes exactly the touched cells); rows (ny * nz ints, may be null)
-// flags the x rows that hold deposited mass, set by the deposit, reset by the clear.
+// CIC deposit of the particles into rho, which must be zero; rows (ny * nz
+// ints, may be null) flags the x rows that hold deposited mass.  The density
+// pass that reads the deposit zeroes the flagged rows and resets their flags.
 cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, int* rows,
                                cudaStream_t st);
-cudaError_t launch_cic_clear(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, int* rows,
-                             cudaStream_t st);
 cudaError_t launch_cic_interp(const float* field, const CicParticle* p, long long n, int nx, int ny, int nz,
                               double* out, cudaStream_t st);
 

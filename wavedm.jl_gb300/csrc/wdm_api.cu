@@ -74,7 +74,6 @@ enum Pass {
   P_KICK,          // final half kick (no FFT)
   P_DENSITY,       // density R2C of real-space psi (start of a run)
   P_CIC_DEPOSIT,
-  P_CIC_CLEAR,
   P_X_FFT,         // plain x-FFT (wdm_drift)
   P_PHI_OUT,       // Phi C2R to a real field
   P_ADJ_KICK,      // adjoint kick: lam x-iFFT, exp(+i th) lam, mu R2C
@@ -84,7 +83,7 @@ enum Pass {
 };
 static const char* const PASS_NAMES[NPASS] = {
     "kick_xfft_fwd", "psi_y_fwd", "psi_z_drift", "psi_y_inv", "psi_x_inv_rho", "rho_y_fwd", "rho_z_poisson",
-    "phi_y_inv",     "kick_final", "rho_density", "cic_deposit", "cic_clear", "psi_x_fwd", "phi_x_c2r",
+    "phi_y_inv",     "kick_final", "rho_density", "cic_deposit", "psi_x_fwd", "phi_x_c2r",
     "adj_kick",   "adj_poisson", "adj_apply"};
 
 struct Profiler {
@@ -237,7 +236,6 @@ static double pass_bytes(const wdm_ctx* c, int p) {
     case P_H_Z_POISSON:
     case P_H_Y_INV: return 16.0 * nh;
     case P_CIC_DEPOSIT: return (double)c->nparts * (sizeof(CicParticle) + 8 * 2 * sizeof(float));
-    case P_CIC_CLEAR: return (double)c->nparts * (sizeof(CicParticle) + 8 * sizeof(float));
     case P_PHI_OUT: return 8.0 * nh + 4.0 * nc;
     case P_ADJ_KICK: return 24.0 * nc + 16.0 * nh;   // lam in/out, pre-kick psi, H in, mu spectrum out
     case P_ADJ_POISSON: return 3.0 * 16.0 * nh;
@@ -442,6 +440,9 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.mz = mask ? c->mz : nullptr;
   ra.rho_b = c->nparts > 0 ? c->rho_b : nullptr;
   ra.rb_rows = c->nparts > 0 ? c->rb_rows : nullptr;
+  // the density pass leaves the deposit zero behind it (no clearing kernel)
+  ra.rb_zero = c->nparts > 0 ? c->rho_b : nullptr;
+  ra.rb_rows_zero = c->nparts > 0 ? c->rb_rows : nullptr;
   ra.rb_bstride = 0;
   ra.write_psi = write_psi;
   ra.nonfinite = c->flag;
@@ -452,12 +453,6 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
                             c->twx, ra, B, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
-  if (c->nparts > 0) {
-    e = run_pass(c, P_CIC_CLEAR, [&] {
-      return launch_cic_clear(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->rb_rows, c->st);
-    });
-    if (e != cudaSuccess) return cuda_fail(c, e, "cic clear");
-  }
   if ((e = run_pass(c, P_H_Y_FWD, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y fwd");

@@ -262,6 +262,7 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
         }
       }
     }
+    if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t);
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
     float2* hrow = H + b * hbstride + ra * hpitch;

@@ -309,6 +309,33 @@ __device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, int b) 
   for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
 }
 
+// After both rows of a pair used their baryon density: zero the flagged rows
+// at the positions this lane read (each lane clears what it read, so no lane
+// races another) and reset the rows' flags.  All lanes of the warp call it;
+// ok selects the lane groups that hold a pair.
+template <int N>
+__device__ __forceinline__ void clear_rb_pair(const RhoArgs& a, const RowGeom& rg, int b, int ra, bool ok, int t) {
+  constexpr int T = XCfg<N>::T;
+  constexpr int RS = RadInfo<typename XPlan<N>::Fwd>::last;
+  __syncwarp();
+  if (ok)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int r = ra + half;
+      if (a.rb_rows && !a.rb_rows[r]) continue;
+      float* row = a.rb_zero + b * a.rb_bstride + (long long)r * rg.pitch;
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = 0.f;
+    }
+  __syncwarp();  // every lane has read the flags before they are reset
+  if (ok && t == 0 && a.rb_rows_zero) {
+    a.rb_rows_zero[ra] = 0;
+    a.rb_rows_zero[ra + 1] = 0;
+  }
+}
+
 template <int N, bool FWD>
 __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGeom rg, long long hpitch,
@@ -424,6 +451,7 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       const float* rb = rb_row ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
       inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t);
     }
+    if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, ok, t);
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
     float2* hrow = H + b * hbstride + ra * hpitch;
