@@ -157,6 +157,11 @@ struct wdm_ctx {
   std::vector<float2*> slot2_psi, slot2_H;              // segment states, set 1
   cudaStream_t st_rec = nullptr;    // adjoint: recompute of the next segment, beside the reverse sweep
   cudaEvent_t ev_ck = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_bwd[2] = {nullptr, nullptr};
+  // baryons: the next density pass's deposit is already in rho_b (made beside
+  // the potential passes of the previous one, on st_cic)
+  int rb_ready = 0;
+  cudaStream_t st_cic = nullptr;
+  cudaEvent_t ev_p5 = nullptr, ev_dep = nullptr;
   // diagnostics: radii histogram and minimum words (allocated on first use)
   double* diag_wsum = nullptr;
   unsigned long long* diag_wmin = nullptr;
@@ -424,14 +429,25 @@ static LineGeom lines_z(const wdm_ctx* c, int xext, long long pitch, long long b
 // density (+baryons) of psi -> H, then the Poisson solve on H (P5..P8).
 // write_psi != 0: psi holds x-spectral data (after P4); the pass inverts it
 // first (with the absorbing mask) and writes real-space psi back.
+// The CIC deposit the next density pass reads, made now on the context stream
+// if none is waiting in rho_b.
+static wdm_status ensure_deposit(wdm_ctx* c) {
+  if (c->nparts == 0 || c->rb_ready) return WDM_OK;
+  cudaError_t e = run_pass(c, P_CIC_DEPOSIT, [&] {
+    return launch_cic_deposit(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->rb_rows, c->st);
+  });
+  if (e != cudaSuccess) return cuda_fail(c, e, "cic deposit");
+  c->rb_ready = 1;
+  return WDM_OK;
+}
+
+// Density pass (P5) and Poisson solve (P6-P8).  With baryons, P5 reads the
+// waiting deposit and leaves rho_b zero; the deposit for the next density pass
+// then runs on st_cic beside P6-P8 (the particles are static, and nothing in
+// between reads rho_b), and the context stream waits for it after P8.
 static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   const int B = c->d.batch;
-  if (c->nparts > 0) {
-    cudaError_t e = run_pass(c, P_CIC_DEPOSIT, [&] {
-      return launch_cic_deposit(c->rho_b, c->parts, c->nparts, c->d.nx, c->d.ny, c->d.nz, c->rb_rows, c->st);
-    });
-    if (e != cudaSuccess) return cuda_fail(c, e, "cic deposit");
-  }
+  if (c->nparts > 0) WDM_TRY(ensure_deposit(c));
   RhoArgs ra{};
   const bool mask = write_psi && c->d.absorb_alpha != 0.0;
   if (mask) WDM_TRY(ensure_mask_tables(c, dt_mask));
@@ -453,6 +469,17 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
                             c->twx, ra, B, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
+  if (c->nparts > 0) {
+    c->rb_ready = 0;
+    WDM_CU(c, cudaEventRecord(c->ev_p5, c->st));
+    WDM_CU(c, cudaStreamWaitEvent(c->st_cic, c->ev_p5, 0));
+    cudaStream_t keep = c->st;
+    c->st = c->st_cic;
+    wdm_status s = ensure_deposit(c);
+    c->st = keep;
+    WDM_TRY(s);
+    WDM_CU(c, cudaEventRecord(c->ev_dep, c->st_cic));
+  }
   if ((e = run_pass(c, P_H_Y_FWD, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y fwd");
@@ -468,6 +495,7 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   if ((e = run_pass(c, P_H_Y_INV, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y inv");
+  if (c->nparts > 0) WDM_CU(c, cudaStreamWaitEvent(c->st, c->ev_dep, 0));
   c->phi_valid = 1;
   return WDM_OK;
 }
@@ -622,6 +650,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   if (c->self_group) wdm_group_destroy(c->self_group);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->st_rec) cudaStreamSynchronize(c->st_rec);
+  if (c->st_cic) cudaStreamSynchronize(c->st_cic);
   void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
                   c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->rb_rows, c->parts, c->T6b, c->flag, c->scratch_f,
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
@@ -634,6 +663,9 @@ wdm_status wdm_destroy(wdm_ctx* c) {
     for (float2* p : *v)
       if (p) cudaFree(p);
   if (c->st_rec) cudaStreamDestroy(c->st_rec);
+  if (c->st_cic) cudaStreamDestroy(c->st_cic);
+  for (cudaEvent_t e : {c->ev_p5, c->ev_dep})
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : {c->ev_ck, c->ev_rec[0], c->ev_rec[1], c->ev_bwd[0], c->ev_bwd[1]})
     if (e) cudaEventDestroy(e);
   for (auto& r : c->prof.pending) {
@@ -961,6 +993,11 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
   if (c->parts) cudaFree(c->parts);
   c->parts = nullptr;
   c->nparts = 0;
+  if (c->rb_ready) {  // a deposit of the old particles is waiting: clear it
+    WDM_CU(c, cudaMemsetAsync(c->rho_b, 0, sizeof(float) * c->ncell, c->st));
+    WDM_CU(c, cudaMemsetAsync(c->rb_rows, 0, sizeof(int) * c->d.ny * c->d.nz, c->st));
+    c->rb_ready = 0;
+  }
   if (n == 0) return WDM_OK;
   if (!pos || !mass) return fail(c, WDM_ERR_INVALID, "null particle arrays");
   if (!c->rho_b) {
@@ -971,6 +1008,9 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
     WDM_TRY(dalloc(c, &c->rb_rows, (size_t)c->d.ny * c->d.nz));
     WDM_CU(c, cudaMemsetAsync(c->rb_rows, 0, sizeof(int) * c->d.ny * c->d.nz, c->st));
   }
+  if (!c->st_cic) WDM_CU(c, cudaStreamCreateWithFlags(&c->st_cic, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&c->ev_p5, &c->ev_dep})
+    if (!*e) WDM_CU(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   // cell index and fractions in FP64 on the host (particles are static)
   std::vector<CicParticle> h((size_t)n);
   const double d[3] = {c->dx, c->dy, c->dz};
@@ -1682,6 +1722,9 @@ static wdm_status prepare_capture(wdm_ctx* c, double dt) {
   if (c->d.phase_mode == WDM_PHASE_PRECISE) WDM_TRY(ensure_drift_tables(c, dt));
   if (c->d.absorb_alpha != 0.0) WDM_TRY(ensure_mask_tables(c, dt));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
+  // a captured sequence assumes a deposit is waiting when it starts (each
+  // density pass leaves the next one), so a replay never deposits twice
+  WDM_TRY(ensure_deposit(c));
   WDM_CU(c, cudaStreamSynchronize(c->st));
   return WDM_OK;
 }
