@@ -215,6 +215,10 @@ void* wdm_stream(wdm_ctx* ctx);
 /* per-pass GPU time: with on != 0 every pass launch is bracketed by CUDA events
  * on the context stream (off by default; turning it on clears the totals) */
 wdm_status wdm_set_profiling(wdm_ctx* ctx, int32_t on);
+/* which passes profiling brackets with events: bit p for pass p (default all).
+ * Bracketing only the pass of interest keeps the event overhead of the others
+ * out of a timed run. */
+wdm_status wdm_set_profile_mask(wdm_ctx* ctx, uint64_t mask);
 /* for pass p < WDM_NPASS: launches, summed milliseconds and algorithmic bytes
  * (one read + one write of every operand) of one launch, since profiling on */
 wdm_status wdm_get_profile(wdm_ctx* ctx, int64_t* launches, double* ms, double* bytes_per_launch);

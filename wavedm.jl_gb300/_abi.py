@@ -72,6 +72,7 @@ SIGNATURES = [
     ("wdm_check_finite", _i32, [_vp, C.POINTER(_i32)]),
     ("wdm_stream", _vp, [_vp]),
     ("wdm_set_profiling", _i32, [_vp, _i32]),
+    ("wdm_set_profile_mask", _i32, [_vp, C.c_uint64]),
     ("wdm_get_profile", _i32, [_vp, _vp, _vp, _vp]),
     ("wdm_num_passes", _i32, []),
     ("wdm_pass_name", C.c_char_p, [_i32]),

@@ -231,6 +231,17 @@ class SPEContext:
     def set_profiling(self, on=True):
         self._check(self.lib.wdm_set_profiling(self.handle, int(bool(on))))
 
+    def set_profile_mask(self, passes=None):
+        """Bracket only the named passes with events while profiling (None: all)."""
+        if passes is None:
+            mask = (1 << 64) - 1
+        else:
+            names = [self.lib.wdm_pass_name(p).decode() for p in range(self.lib.wdm_num_passes())]
+            mask = 0
+            for name in passes:
+                mask |= 1 << names.index(name)
+        self._check(self.lib.wdm_set_profile_mask(self.handle, C.c_uint64(mask)))
+
     def profile(self):
         """{pass name: dict(launches, ms, bytes_per_launch)} since profiling was turned on."""
         n = self.lib.wdm_num_passes()

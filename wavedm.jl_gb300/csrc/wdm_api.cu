@@ -88,6 +88,7 @@ static const char* const PASS_NAMES[NPASS] = {
 
 struct Profiler {
   bool on = false;
+  uint64_t mask = ~0ull;  // passes bracketed by events while on (bit p: pass p)
   std::vector<cudaEvent_t> pool;
   struct Rec {
     int pass;
@@ -211,7 +212,7 @@ static cudaError_t counted(wdm_ctx* c, F launch) {
 
 template <class F>
 static cudaError_t run_pass(wdm_ctx* c, int pass, F launch) {
-  if (!c->prof.on) return counted(c, launch);
+  if (!c->prof.on || !((c->prof.mask >> pass) & 1ull)) return counted(c, launch);
   cudaEvent_t a = prof_event(c), b = prof_event(c);
   cudaEventRecord(a, c->st);
   cudaError_t e = counted(c, launch);
@@ -1451,6 +1452,12 @@ wdm_status wdm_set_profiling(wdm_ctx* c, int32_t on) {
     c->prof.ms[p] = 0.0;
   }
   c->prof.on = on != 0;
+  return WDM_OK;
+}
+
+wdm_status wdm_set_profile_mask(wdm_ctx* c, uint64_t mask) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  c->prof.mask = mask;
   return WDM_OK;
 }
 
