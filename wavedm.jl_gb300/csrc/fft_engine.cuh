@@ -285,6 +285,29 @@ __device__ __forceinline__ void stage_compute(float2* v, const float4* __restric
   }
 }
 
+// stage_compute on two lines at once, sharing each twiddle load.
+template <int N, int T, int R, int NS, bool INV, int OFF>
+__device__ __forceinline__ void stage_compute2(float2* va, float2* vb, const float4* __restrict__ tw, int t) {
+  constexpr int NB = N / (R * T);
+  static_assert(NB * R * T == N, "plan: T must divide N/R");
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    if constexpr (NS > 1) {
+      const int j = t + T * i;
+      const int jm = j % NS;
+      const float4* w = tw + OFF + jm * (R - 1);
+#pragma unroll
+      for (int k = 1; k < R; ++k) {
+        const float4 wk = w[k - 1];
+        va[i * R + k] = twiddle_mul<(NS * R) % 12 == 0>(va[i * R + k], wk, INV);
+        vb[i * R + k] = twiddle_mul<(NS * R) % 12 == 0>(vb[i * R + k], wk, INV);
+      }
+    }
+    dftR<R, INV>(va + i * R);
+    dftR<R, INV>(vb + i * R);
+  }
+}
+
 // Host-side builder of the stage-major twiddle table of a radix order
 // (W_N^m in FP64, stored as FP32 hi + lo); writes N - 1 entries.
 template <int N, class TW, class F, int... Rs>

@@ -16,6 +16,11 @@
 #pragma once
 #include "xpass_warp.cuh"
 
+// 1: the staged kick transforms the two rows of a pair side by side
+#ifndef WDM_XS_PAIR
+#define WDM_XS_PAIR 1
+#endif
+
 namespace wdm {
 
 template <int N>
@@ -37,6 +42,7 @@ struct XStage {
   static constexpr int MINB_RAW = (int)((228u * 1024u) / (SMEM + 1024u));
   static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
   static_assert(BASE % 16 == 0 && A_BYTES % 16 == 0 && B_BYTES % 16 == 0, "16-byte aligned slots");
+  static_assert(2 * PSI_P >= C::NP, "a pair's psi rows hold one exchange buffer");
 };
 
 // Copy `nrows` rows of `row_elems` elements (pitch src_pitch) to a slot with
@@ -159,6 +165,42 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
     }
     float T6[6];
     kick_tidal<N>(T6, a, b);
+    auto release_b = [&]() {
+      xrelease();
+      if (un < nunits) {
+        if (lane == 0) issue_p(un);
+        pend |= 2u;
+      }
+    };
+#if WDM_XS_PAIR
+    // Both rows of the pair at once.  With FWD, slot B (whose rows are then in
+    // registers) is row B's exchange buffer, so the next unit's psi copy is
+    // issued after the transforms; it still lands under the next potential
+    // transform.
+    if (!WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
+    float2 vb[N / T];
+    float2* sb = slotB + (2 * g) * S::PSI_P;
+#pragma unroll
+    for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+      for (int k = 0; k < R1; ++k) {
+        v[i * R1 + k] = sb[slot_pos<N, T, R1>(t, i, k)];
+        vb[i * R1 + k] = sb[S::PSI_P + slot_pos<N, T, R1>(t, i, k)];
+      }
+    if constexpr (!FWD) release_b();
+    kick_points<N>(v, phi[0], T6, a, rg, ra, b, true, t);
+    kick_points<N>(vb, phi[1], T6, a, rg, ra + 1, b, true, t);
+    float2* rowa = psi + b * rg.bstride + (long long)ra * rg.pitch;
+    if constexpr (FWD) {
+      run_wstages2<N, T, C::NP, false>(Rad{}, v, vb, buf, sb, tw, t);
+      store_row<N, RS>(rowa, v, true, t);
+      store_row<N, RS>(rowa + rg.pitch, vb, true, t);
+      release_b();
+    } else {
+      store_row<N, R1>(rowa, v, true, t);
+      store_row<N, R1>(rowa + rg.pitch, vb, true, t);
+    }
+#else
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       if (half == 0 && !WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
@@ -167,17 +209,12 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       for (int i = 0; i < N / (R1 * T); ++i)
 #pragma unroll
         for (int k = 0; k < R1; ++k) v[i * R1 + k] = srow[slot_pos<N, T, R1>(t, i, k)];
-      if (half == 1) {
-        xrelease();
-        if (un < nunits) {
-          if (lane == 0) issue_p(un);
-          pend |= 2u;
-        }
-      }
+      if (half == 1) release_b();
       const int r = ra + half;
       kick_row<N, FWD>(v, phi[half], T6, a, rg, r, b, true, psi + b * rg.bstride + (long long)r * rg.pitch, buf, tw,
                        t);
     }
+#endif
   }
 }
 
@@ -227,6 +264,45 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     float2 z[N / T];    // packed (rho_A, rho_B) at radix-RS slots
     float2 v[N / T];
     if (!WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
+    auto release_p = [&]() {
+      xrelease();
+      if (un < nunits) {
+        if (lane == 0) issue_p(un);
+        pend |= 2u;
+      }
+    };
+    auto release_r = [&]() {
+      xrelease();
+      if (un < nunits) {
+        if (lane == 0) issue_r(un);
+        pend |= 1u;
+      }
+    };
+    auto rb_of = [&](int half) -> const float* {
+      const bool rb_row = with_rb && (!a.rb_rows || a.rb_rows[ra + half]);
+      return rb_row ? rbslot + (2 * g + half) * S::RB_P : nullptr;
+    };
+    const bool paired = WDM_XS_PAIR && a.write_psi;
+    if (paired) {
+      // Both rows inverted side by side, row B exchanging through slot B
+      // (its rows are in registers by then); the next psi copy follows.
+      float2 vb[N / T];
+      float2* sb = slotB + (2 * g) * S::PSI_P;
+#pragma unroll
+      for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+        for (int k = 0; k < R1; ++k) {
+          v[i * R1 + k] = sb[slot_pos<N, T, R1>(t, i, k)];
+          vb[i * R1 + k] = sb[S::PSI_P + slot_pos<N, T, R1>(t, i, k)];
+        }
+      run_wstages2<N, T, C::NP, true>(Rad{}, v, vb, buf, sb, tw, t);
+      release_p();
+      if (with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
+      float2* rowa = psi + b * rg.bstride + (long long)ra * rg.pitch;
+      rho_row_post<N>(v, a, rg, ra, true, rowa, rb_of(0), shift, 0, rho0, z, t);
+      rho_row_post<N>(vb, a, rg, ra + 1, true, rowa + rg.pitch, rb_of(1), shift, 1, rho0, z, t);
+      if (with_rb) release_r();
+    } else {
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const float2* srow = slotB + (2 * g + half) * S::PSI_P;
@@ -241,26 +317,13 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
 #pragma unroll
           for (int k = 0; k < RS; ++k) v[i * RS + k] = srow[slot_pos<N, T, RS>(t, i, k)];
       }
-      if (half == 1) {
-        xrelease();
-        if (un < nunits) {
-          if (lane == 0) issue_p(un);
-          pend |= 2u;
-        }
-      }
+      if (half == 1) release_p();
       if (half == 0 && with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
       const int r = ra + half;
-      const bool rb_row = with_rb && (!a.rb_rows || a.rb_rows[r]);
-      const float* rb = rb_row ? rbslot + (2 * g + half) * S::RB_P : nullptr;
-      inv_rho_row<N>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb, shift, half, rho0, z,
-                     buf, tw, t);
-      if (half == 1 && with_rb) {
-        xrelease();
-        if (un < nunits) {
-          if (lane == 0) issue_r(un);
-          pend |= 1u;
-        }
-      }
+      inv_rho_row<N>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb_of(half), shift, half,
+                     rho0, z, buf, tw, t);
+      if (half == 1 && with_rb) release_r();
+    }
     }
     if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t);
     reorder<N, T, RS, R1>(z, v);

@@ -135,6 +135,33 @@ __device__ __forceinline__ void run_wstages(Radices<Rs...>, float2* v, float2* b
   run_wstages_impl<N, T, NP, INV, 1, 0, Rs...>(v, b, tw, t);
 }
 
+// Two rows through the same stages side by side (row A exchanging through ba,
+// row B through bb): each twiddle is loaded once for both rows and each stage
+// boundary costs one pair of warp barriers, with two independent chains of
+// arithmetic in flight.
+template <int N, int T, int NP, bool INV, int NS, int OFF, int R, int... Rest>
+__device__ __forceinline__ void run_wstages2_impl(float2* va, float2* vb, float2* ba, float2* bb, const float4* tw,
+                                                  int t) {
+  stage_compute2<N, T, R, NS, INV, OFF>(va, vb, tw, t);
+  if constexpr (sizeof...(Rest) > 0) {
+    constexpr int RN = First<Rest...>::value;
+    constexpr int SH = XPad<N, T, NP>::best(R, NS, RN);
+    __syncwarp();
+    wstage_write<N, T, R, NS, SH>(ba, va, t);
+    wstage_write<N, T, R, NS, SH>(bb, vb, t);
+    __syncwarp();
+    wstage_read<N, T, RN, SH>(ba, va, t);
+    wstage_read<N, T, RN, SH>(bb, vb, t);
+    run_wstages2_impl<N, T, NP, INV, NS * R, OFF + NS * (R - 1), Rest...>(va, vb, ba, bb, tw, t);
+  }
+}
+
+template <int N, int T, int NP, bool INV, int... Rs>
+__device__ __forceinline__ void run_wstages2(Radices<Rs...>, float2* va, float2* vb, float2* ba, float2* bb,
+                                             const float4* tw, int t) {
+  run_wstages2_impl<N, T, NP, INV, 1, 0, Rs...>(va, vb, ba, bb, tw, t);
+}
+
 // Register slot q = i R + k holds point slot_pos<R>(t, i, k) = t + T (i + k N/(R T)).
 // reorder<RA, RB>: registers positioned for radix RA -> positioned for RB
 // (the same set of points t + T m, only the slot order differs).
@@ -255,17 +282,14 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
 // ----------------------------------------------------------------------------
 // P1: Phi rows from H (C2R of the packed pair), kick, forward x-FFT (or not)
 // ----------------------------------------------------------------------------
-// One row of the kick pass: v holds psi row r at radix-R1 slots, phi its
-// potential at the same slots; kick, then (FWD) the forward x transform, and
-// store to `row` (when ok).  Shared by the direct and the staged kernels.
-template <int N, bool FWD>
-__device__ __forceinline__ void kick_row(float2* v, const float* phi, const float* T6, const KickArgs& a,
-                                         const RowGeom& rg, int r, int b, bool ok, float2* row, float2* buf,
-                                         const float4* tw, int t) {
+// The kick of one row: v holds psi row r at radix-R1 slots, phi its potential
+// at the same slots; v <- v exp(-i dt pot).
+template <int N>
+__device__ __forceinline__ void kick_points(float2* v, const float* phi, const float* T6, const KickArgs& a,
+                                            const RowGeom& rg, int r, int b, bool ok, int t) {
   using C = XCfg<N>;
   constexpr int T = C::T;
-  using Rad = typename XPlan<N>::Fwd;
-  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
+  constexpr int R1 = RadInfo<typename XPlan<N>::Fwd>::first;
   const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
   const int y = r % rg.ny, z = r / rg.ny;
   const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * z;
@@ -287,19 +311,35 @@ __device__ __forceinline__ void kick_row(float2* v, const float* phi, const floa
       if (vrow && ok) pot += vrow[x];
       v[q] = apply_kick(v[q], pot, a);
     }
+}
+
+// Store a row held at radix-R slots (when ok).
+template <int N, int R>
+__device__ __forceinline__ void store_row(float2* row, const float2* v, bool ok, int t) {
+  constexpr int T = XCfg<N>::T;
+  if (!ok) return;
+#pragma unroll
+  for (int i = 0; i < N / (R * T); ++i)
+#pragma unroll
+    for (int k = 0; k < R; ++k) row[slot_pos<N, T, R>(t, i, k)] = v[i * R + k];
+}
+
+// One row of the kick pass: kick, then (FWD) the forward x transform, and
+// store to `row` (when ok).  Used by the direct kernel.
+template <int N, bool FWD>
+__device__ __forceinline__ void kick_row(float2* v, const float* phi, const float* T6, const KickArgs& a,
+                                         const RowGeom& rg, int r, int b, bool ok, float2* row, float2* buf,
+                                         const float4* tw, int t) {
+  using C = XCfg<N>;
+  constexpr int T = C::T;
+  using Rad = typename XPlan<N>::Fwd;
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
+  kick_points<N>(v, phi, T6, a, rg, r, b, ok, t);
   if constexpr (FWD) {
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
-    if (ok)
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+    store_row<N, RS>(row, v, ok, t);
   } else {
-    if (ok)
-#pragma unroll
-      for (int i = 0; i < N / (R1 * T); ++i)
-#pragma unroll
-        for (int k = 0; k < R1; ++k) row[slot_pos<N, T, R1>(t, i, k)] = v[i * R1 + k];
+    store_row<N, R1>(row, v, ok, t);
   }
 }
 
@@ -377,20 +417,17 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
 // P5: psi x-inverse (+mask) of rows A and B, rho = |psi|^2 (+rho_b) - shift,
 // packed R2C of (rho_A, rho_B) -> H rows A and B
 // ----------------------------------------------------------------------------
-// One row of P5: v holds psi row r (write_psi: x-spectral at radix-R1 slots,
-// else real space at radix-RS slots).  Inverts it (+mask) and stores it back
-// to `row` (write_psi), then forms rho - shift at radix-RS slots into rho0
-// (half 0) or the packed z (half 1).  rb: the baryon density row or null.
+// The part of a P5 row after its inverse transform: v holds psi row r in real
+// space at radix-RS slots; mask it and store it back to `row` (write_psi), then
+// form rho - shift into rho0 (half 0) or the packed z (half 1).  rb: the
+// baryon density row or null.
 template <int N>
-__device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
-                                            float2* row, const float* rb, float shift, int half, float* rho0,
-                                            float2* z, float2* buf, const float4* tw, int t) {
-  using C = XCfg<N>;
-  constexpr int T = C::T;
-  using Rad = typename XPlan<N>::Fwd;
-  constexpr int RS = RadInfo<Rad>::last;
+__device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
+                                             float2* row, const float* rb, float shift, int half, float* rho0,
+                                             float2* z, int t) {
+  constexpr int T = XCfg<N>::T;
+  constexpr int RS = RadInfo<typename XPlan<N>::Fwd>::last;
   if (a.write_psi) {
-    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
     if (a.mx) {
       const int y = r % rg.ny, zz = r / rg.ny;
       const float myz = ok ? a.my[y] * a.mz[zz] : 0.f;
@@ -399,11 +436,7 @@ __device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const R
 #pragma unroll
         for (int k = 0; k < RS; ++k) v[i * RS + k] = cscale(v[i * RS + k], myz * a.mx[slot_pos<N, T, RS>(t, i, k)]);
     }
-    if (ok)
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = v[i * RS + k];
+    store_row<N, RS>(row, v, ok, t);
   }
 #pragma unroll
   for (int i = 0; i < N / (RS * T); ++i)
@@ -416,6 +449,18 @@ __device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const R
       if (half == 0) rho0[i * RS + k] = d - shift;
       else z[i * RS + k] = make_float2(rho0[i * RS + k], d - shift);
     }
+}
+
+// One row of P5: v holds psi row r (write_psi: x-spectral at radix-R1 slots,
+// else real space at radix-RS slots).  Inverts it (write_psi), then
+// rho_row_post.
+template <int N>
+__device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
+                                            float2* row, const float* rb, float shift, int half, float* rho0,
+                                            float2* z, float2* buf, const float4* tw, int t) {
+  using C = XCfg<N>;
+  if (a.write_psi) run_wstages<N, C::T, C::NP, true>(typename XPlan<N>::Fwd{}, v, buf, tw, t);
+  rho_row_post<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, t);
 }
 
 template <int N>
