@@ -16,7 +16,7 @@
 #pragma once
 #include "xpass_warp.cuh"
 
-// 1: the staged kick transforms the two rows of a pair side by side
+// 1: the staged x passes transform the two rows of a pair side by side
 #ifndef WDM_XS_PAIR
 #define WDM_XS_PAIR 1
 #endif
@@ -173,13 +173,16 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       }
     };
 #if WDM_XS_PAIR
-    // Both rows of the pair at once.  With FWD, slot B (whose rows are then in
-    // registers) is row B's exchange buffer, so the next unit's psi copy is
-    // issued after the transforms; it still lands under the next potential
-    // transform.
+    // Both rows of the pair at once: one twiddle load per entry for both
+    // transforms, which exchange through the group buffer in turn, so that
+    // slot B is free for the next unit's psi copy as soon as its rows are in
+    // registers.  (Row B exchanging through slot B instead, which delays that
+    // copy until after the transforms, measured 1% slower at N = 384; the
+    // density pass, whose next psi copy has the R2C transform to land under,
+    // uses that form.)
     if (!WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
     float2 vb[N / T];
-    float2* sb = slotB + (2 * g) * S::PSI_P;
+    const float2* sb = slotB + (2 * g) * S::PSI_P;
 #pragma unroll
     for (int i = 0; i < N / (R1 * T); ++i)
 #pragma unroll
@@ -187,15 +190,14 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
         v[i * R1 + k] = sb[slot_pos<N, T, R1>(t, i, k)];
         vb[i * R1 + k] = sb[S::PSI_P + slot_pos<N, T, R1>(t, i, k)];
       }
-    if constexpr (!FWD) release_b();
+    release_b();
     kick_points<N>(v, phi[0], T6, a, rg, ra, b, true, t);
     kick_points<N>(vb, phi[1], T6, a, rg, ra + 1, b, true, t);
     float2* rowa = psi + b * rg.bstride + (long long)ra * rg.pitch;
     if constexpr (FWD) {
-      run_wstages2<N, T, C::NP, false>(Rad{}, v, vb, buf, sb, tw, t);
+      run_wstages2<N, T, C::NP, false, true>(Rad{}, v, vb, buf, buf, tw, t);
       store_row<N, RS>(rowa, v, true, t);
       store_row<N, RS>(rowa + rg.pitch, vb, true, t);
-      release_b();
     } else {
       store_row<N, R1>(rowa, v, true, t);
       store_row<N, R1>(rowa + rg.pitch, vb, true, t);
