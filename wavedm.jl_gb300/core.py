@@ -239,6 +239,8 @@ class SPEContext:
             names = [self.lib.wdm_pass_name(p).decode() for p in range(self.lib.wdm_num_passes())]
             mask = 0
             for name in passes:
+                if name not in names:
+                    raise ValueError(f"unknown pass {name!r}; passes: {names}")
                 mask |= 1 << names.index(name)
         self._check(self.lib.wdm_set_profile_mask(self.handle, C.c_uint64(mask)))
 
