@@ -129,9 +129,8 @@ struct DriftOp {
       return make_float2(fmaf(w.x, scale, w.x * scale_lo), fmaf(w.y, scale, w.y * scale_lo));
     }
     const float th = sign * (kx2[mx] + ky2[my] + kz2[pos]) * half_dt;
-    float s, c;
-    sincosf(th, &s, &c);
-    return cmul(v, make_float2(c * scale, -s * scale));
+    const float2 sc = sincos_plain(th);
+    return cmul(v, make_float2(sc.y * scale, -sc.x * scale));
   }
 };
 
@@ -499,9 +498,8 @@ __device__ __forceinline__ float2 kick_factor(float pot, const KickArgs& a) {
     const float r = fmaf(-n, 6.28318548202514648f, th) + fmaf(-n, -1.7484555e-07f, te);
     return expm1_neg_i(r);  // (cos r - 1, -sin r)
   }
-  float s, c;
-  sincosf(pot * a.dt_hi, &s, &c);
-  return make_float2(c, -s);
+  const float2 sc = sincos_plain(pot * a.dt_hi);
+  return make_float2(sc.y, -sc.x);
 }
 
 // v exp(-i th), or v exp(+i th) (CONJ), from the factor of kick_factor.  In

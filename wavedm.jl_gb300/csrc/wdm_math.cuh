@@ -30,6 +30,17 @@ __device__ __forceinline__ void sincos_half(float h, float* s, float* c) {
   *c = fmaf(x2, pc, 1.f);
 }
 
+// (sin th, cos th) of the plain phase form: one FP32 sincosf, kept out of line.
+// Inlined at every point of the unrolled kick and drift loops, its range
+// reduction (with the slow path for large arguments) made those kernels about
+// twice as large, and the precise form, which shares the kernels, paid for it
+// in instruction-cache misses.
+static __device__ __noinline__ float2 sincos_plain(float th) {
+  float s, c;
+  sincosf(th, &s, &c);
+  return make_float2(s, c);
+}
+
 // exp(-i r) - 1 = (-2 sin^2(r/2), -2 sin(r/2) cos(r/2)) for |r| <= pi, accurate
 // relative to |exp(-i r) - 1| (no cancellation for small r).
 __device__ __forceinline__ float2 expm1_neg_i(float r) {
