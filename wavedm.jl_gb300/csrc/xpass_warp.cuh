@@ -139,8 +139,7 @@ __device__ __forceinline__ void run_wstages(Radices<Rs...>, float2* v, float2* b
 // row B through bb): each twiddle is loaded once for both rows and each stage
 // boundary costs one pair of warp barriers, with two independent chains of
 // arithmetic in flight.
-// ONEBUF: both rows exchange through ba, one after the other.
-template <int N, int T, int NP, bool INV, bool ONEBUF, int NS, int OFF, int R, int... Rest>
+template <int N, int T, int NP, bool INV, int NS, int OFF, int R, int... Rest>
 __device__ __forceinline__ void run_wstages2_impl(float2* va, float2* vb, float2* ba, float2* bb, const float4* tw,
                                                   int t) {
   stage_compute2<N, T, R, NS, INV, OFF>(va, vb, tw, t);
@@ -149,25 +148,18 @@ __device__ __forceinline__ void run_wstages2_impl(float2* va, float2* vb, float2
     constexpr int SH = XPad<N, T, NP>::best(R, NS, RN);
     __syncwarp();
     wstage_write<N, T, R, NS, SH>(ba, va, t);
-    if constexpr (!ONEBUF) wstage_write<N, T, R, NS, SH>(bb, vb, t);
+    wstage_write<N, T, R, NS, SH>(bb, vb, t);
     __syncwarp();
     wstage_read<N, T, RN, SH>(ba, va, t);
-    if constexpr (ONEBUF) {
-      __syncwarp();
-      wstage_write<N, T, R, NS, SH>(ba, vb, t);
-      __syncwarp();
-      wstage_read<N, T, RN, SH>(ba, vb, t);
-    } else {
-      wstage_read<N, T, RN, SH>(bb, vb, t);
-    }
-    run_wstages2_impl<N, T, NP, INV, ONEBUF, NS * R, OFF + NS * (R - 1), Rest...>(va, vb, ba, bb, tw, t);
+    wstage_read<N, T, RN, SH>(bb, vb, t);
+    run_wstages2_impl<N, T, NP, INV, NS * R, OFF + NS * (R - 1), Rest...>(va, vb, ba, bb, tw, t);
   }
 }
 
-template <int N, int T, int NP, bool INV, bool ONEBUF = false, int... Rs>
+template <int N, int T, int NP, bool INV, int... Rs>
 __device__ __forceinline__ void run_wstages2(Radices<Rs...>, float2* va, float2* vb, float2* ba, float2* bb,
                                              const float4* tw, int t) {
-  run_wstages2_impl<N, T, NP, INV, ONEBUF, 1, 0, Rs...>(va, vb, ba, bb, tw, t);
+  run_wstages2_impl<N, T, NP, INV, 1, 0, Rs...>(va, vb, ba, bb, tw, t);
 }
 
 // Register slot q = i R + k holds point slot_pos<R>(t, i, k) = t + T (i + k N/(R T)).
