@@ -43,9 +43,9 @@ B_ALG_PER_CELL = 192.0  # 4 C2C 3D FFTs x 3 axis passes x (8 B read + 8 B write)
 # pass, from the ncu captures of the 384^3 workload with the tuned schedule
 # (summarised under profiles/): (pass, kernel implementation) -> bytes.
 NCU_TRAFFIC_384 = {
-    ("kick_xfft_fwd", "staged"): 1077.1e6,
+    ("kick_xfft_fwd", "staged"): 1077.4e6,
     ("kick_final", "staged"): 1077.3e6,
-    ("psi_z_drift", "tma"): 845.1e6,
+    ("psi_z_drift", "tma"): 844.5e6,
     ("psi_x_inv_rho", "staged"): 1104.9e6,
     ("rho_y_fwd", "tma"): 401.5e6,
     ("rho_z_poisson", "tma"): 401.6e6,
