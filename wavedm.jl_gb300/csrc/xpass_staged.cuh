@@ -231,31 +231,42 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     unit_rows(u, C::GROUPS, ppi, &b, &ra);
     stage_rows(slotB, S::PSI_P, psi + b * rg.bstride + ra * rg.pitch, rg.pitch, N, S::ROWS, &xbar[1]);
   };
+  const bool with_rb = a.rho_b != nullptr;
+  // Bit r: row r of unit uu holds baryon mass (every row without flags).  The
+  // flags are read a unit ahead, so that their latency hides under the work
+  // of a unit instead of stalling the copies and the density.
+  auto rb_mask = [&](long long uu) -> unsigned {
+    if (!with_rb) return 0u;
+    if (!a.rb_rows) return (1u << S::ROWS) - 1u;
+    int b, ra0;
+    unit_rows(uu, C::GROUPS, ppi, &b, &ra0);
+    unsigned m = 0;
+#pragma unroll
+    for (int r = 0; r < S::ROWS; ++r) m |= (a.rb_rows[ra0 + r] ? 1u : 0u) << r;
+    return m;
+  };
   // only the rows flagged as holding baryon mass are copied (a phase with no
   // copy completes on the arrival alone)
-  auto issue_r = [&](long long u) {
+  auto issue_r = [&](long long u, unsigned m) {
     int b, ra;
     unit_rows(u, C::GROUPS, ppi, &b, &ra);
     const float* src = a.rho_b + b * a.rb_bstride + ra * rg.pitch;
-    unsigned bytes = 0;
+    mbar_expect_tx(&xbar[0], (unsigned)__popc(m) * (unsigned)(N * sizeof(float)));
     for (int r = 0; r < S::ROWS; ++r)
-      if (!a.rb_rows || a.rb_rows[ra + r]) bytes += (unsigned)(N * sizeof(float));
-    mbar_expect_tx(&xbar[0], bytes);
-    for (int r = 0; r < S::ROWS; ++r)
-      if (!a.rb_rows || a.rb_rows[ra + r])
-        bulk_g2s(rbslot + r * S::RB_P, src + r * rg.pitch, (unsigned)(N * sizeof(float)), &xbar[0]);
+      if ((m >> r) & 1u) bulk_g2s(rbslot + r * S::RB_P, src + r * rg.pitch, (unsigned)(N * sizeof(float)), &xbar[0]);
   };
-  const bool with_rb = a.rho_b != nullptr;
   long long u = (long long)blockIdx.x * C::WARPS + warp;
+  unsigned mcur = u < nunits ? rb_mask(u) : 0u;
   if (u < nunits) {
     if (lane == 0) {
       issue_p(u);
-      if (with_rb) issue_r(u);
+      if (with_rb) issue_r(u, mcur);
     }
     pend = with_rb ? 3u : 2u;
   }
   for (; u < nunits; u += wstride) {
     const long long un = u + wstride;
+    const unsigned mnext = un < nunits ? rb_mask(un) : 0u;
     int b, ra;
     unit_rows(u, C::GROUPS, ppi, &b, &ra);
     ra += 2 * g;
@@ -274,13 +285,12 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     auto release_r = [&]() {
       xrelease();
       if (un < nunits) {
-        if (lane == 0) issue_r(un);
+        if (lane == 0) issue_r(un, mnext);
         pend |= 1u;
       }
     };
     auto rb_of = [&](int half) -> const float* {
-      const bool rb_row = with_rb && (!a.rb_rows || a.rb_rows[ra + half]);
-      return rb_row ? rbslot + (2 * g + half) * S::RB_P : nullptr;
+      return ((mcur >> (2 * g + half)) & 1u) ? rbslot + (2 * g + half) * S::RB_P : nullptr;
     };
     const bool paired = WDM_XS_PAIR && a.write_psi;
     if (paired) {
@@ -325,7 +335,8 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       if (half == 1 && with_rb) release_r();
     }
     }
-    if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t);
+    if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t, (mcur >> (2 * g)) & 3u);
+    mcur = mnext;
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
     float2* hrow = H + b * hbstride + ra * hpitch;

@@ -352,9 +352,11 @@ __device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, int b) 
 // After both rows of a pair used their baryon density: zero the flagged rows
 // at the positions this lane read (each lane clears what it read, so no lane
 // races another) and reset the rows' flags.  All lanes of the warp call it;
-// ok selects the lane groups that hold a pair.
+// ok selects the lane groups that hold a pair.  flags: bit h set when row
+// ra + h is flagged (both bits without flags).
 template <int N>
-__device__ __forceinline__ void clear_rb_pair(const RhoArgs& a, const RowGeom& rg, int b, int ra, bool ok, int t) {
+__device__ __forceinline__ void clear_rb_pair(const RhoArgs& a, const RowGeom& rg, int b, int ra, bool ok, int t,
+                                              unsigned flags) {
   constexpr int T = XCfg<N>::T;
   constexpr int RS = RadInfo<typename XPlan<N>::Fwd>::last;
   __syncwarp();
@@ -362,7 +364,7 @@ __device__ __forceinline__ void clear_rb_pair(const RhoArgs& a, const RowGeom& r
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const int r = ra + half;
-      if (a.rb_rows && !a.rb_rows[r]) continue;
+      if (!((flags >> half) & 1u)) continue;
       float* row = a.rb_zero + b * a.rb_bstride + (long long)r * rg.pitch;
 #pragma unroll
       for (int i = 0; i < N / (RS * T); ++i)
@@ -496,7 +498,10 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       const float* rb = rb_row ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
       inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t);
     }
-    if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, ok, t);
+    if (a.rb_zero) {
+      const unsigned fl = ok ? (!a.rb_rows ? 3u : (a.rb_rows[ra] ? 1u : 0u) | (a.rb_rows[ra + 1] ? 2u : 0u)) : 0u;
+      clear_rb_pair<N>(a, rg, b, ra, ok, t, fl);
+    }
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
     float2* hrow = H + b * hbstride + ra * hpitch;
