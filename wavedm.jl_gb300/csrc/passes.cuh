@@ -113,6 +113,7 @@ struct DriftOp {
   float sign;             // +1: exp(-i k^2 dt/2); -1: its conjugate (the drift adjoint)
   int precise;
   long long tab_bstride;  // per-batch-item stride of the phase tables (0 = shared)
+  static constexpr bool TABLE = false;
   __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int b) const {
     if (precise) {
       const long long o = b * tab_bstride;
@@ -140,7 +141,17 @@ struct PoissonOp {
   const float* kz2;
   float coef;  // -c / (nx ny nz)
   __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int) const {
-    const float k2 = kx2[mx] + ky2[my] + kz2[pos];
+    return scaled(v, kx2[mx] + ky2[my] + kz2[pos]);
+  }
+  // The TMA line pass stages kz2 (the table along its lines) in shared memory
+  // once per CTA: read from global memory between the two transforms of every
+  // point, with nothing to hide its latency, it was the pass's main stall.
+  static constexpr bool TABLE = true;
+  __device__ __forceinline__ float table_entry(int pos) const { return kz2[pos]; }
+  __device__ __forceinline__ float2 with_table(float2 v, int mx, int my, int pos, const float* tab) const {
+    return scaled(v, kx2[mx] + ky2[my] + tab[pos]);
+  }
+  __device__ __forceinline__ float2 scaled(float2 v, float k2) const {
     const float f = (k2 > 0.f) ? coef / k2 : 0.f;
     return make_float2(v.x * f, v.y * f);
   }
@@ -258,6 +269,7 @@ k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
 }
 
 struct NoOp {
+  static constexpr bool TABLE = false;
   __device__ __forceinline__ float2 operator()(float2 v, int, int, int, int) const { return v; }
 };
 
@@ -329,8 +341,9 @@ struct TmaTile {
 
 template <int N, int MODE>
 __host__ __device__ constexpr size_t ltma_smem_bytes() {
-  // two tile slots, the twiddle table(s), two mbarriers
-  return 2 * (size_t)TmaTile<N>::BYTES + sizeof(float4) * (MODE == 2 ? 2 : 1) * N + 2 * sizeof(uint64_t);
+  // two tile slots, the twiddle table(s), two mbarriers (, an operator table)
+  return 2 * (size_t)TmaTile<N>::BYTES + sizeof(float4) * (MODE == 2 ? 2 : 1) * N + 2 * sizeof(uint64_t) +
+         (MODE == 2 ? sizeof(float) * N : 0);
 }
 
 template <int N>
@@ -371,6 +384,7 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
   float2* slots = reinterpret_cast<float2*>(lsm);
   float4* tw = reinterpret_cast<float4*>(lsm + 2 * TT::BYTES);
   uint64_t* bar = reinterpret_cast<uint64_t*>(lsm + 2 * TT::BYTES + sizeof(float4) * NTAB * N);
+  float* optab = reinterpret_cast<float*>(bar + 2);  // N entries (MODE 2)
   const int tid = threadIdx.x;
   const int l = tid % LINES, t = tid / LINES;
   // tiles of 16 columns; when 16 does not divide nxa the last tile of a row
@@ -384,6 +398,8 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
     mbar_fence_init();
   }
   load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
+  if constexpr (MODE == 2 && Op::TABLE)
+    for (int i = tid; i < N; i += blockDim.x) optab[i] = op.table_entry(i);
   __syncthreads();
   long long tile = blockIdx.x;
   if (tid == 0 && tile < total) ltma_issue<N>(&map, slots, &bar[0], g, tile, tx);
@@ -424,7 +440,12 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
 #pragma unroll
       for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], g.x0 + mx, row, slot_pos<N, T, RS>(t, i, k), b);
+        for (int k = 0; k < RS; ++k) {
+          if constexpr (Op::TABLE)
+            v[i * RS + k] = op.with_table(v[i * RS + k], g.x0 + mx, row, slot_pos<N, T, RS>(t, i, k), optab);
+          else
+            v[i * RS + k] = op(v[i * RS + k], g.x0 + mx, row, slot_pos<N, T, RS>(t, i, k), b);
+        }
       run_stages<N, T, LINES, true>(Rev{}, v, s, tw + N, t, l);
       lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
     } else {
