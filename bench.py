@@ -39,29 +39,64 @@ sys.path.insert(0, ROOT)
 
 B_ALG_PER_CELL = 192.0  # 4 C2C 3D FFTs x 3 axis passes x (8 B read + 8 B write) of complex64
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
-# pass, from the ncu captures of the 384^3 workload with the tuned schedule
-# (summarised under profiles/): (pass, kernel implementation) -> bytes.
-NCU_TRAFFIC_384 = {
-    ("kick_xfft_fwd", "staged"): 1077.4e6,
-    ("kick_final", "staged"): 1077.3e6,
-    ("psi_z_drift", "tma"): 844.5e6,
-    ("psi_x_inv_rho", "staged"): 1104.9e6,
-    ("rho_y_fwd", "tma"): 401.5e6,
-    ("rho_z_poisson", "tma"): 401.6e6,
-    ("phi_y_inv", "tma"): 401.6e6,
-}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
+# pass, read from the ncu capture summarised in this file, together with the
+# hash of the kernel sources it was captured on.
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "step384_traffic.json")
+CSRC = os.path.join(ROOT, "wavedm.jl_gb300", "csrc")
+
+
+def kernel_source_hash():
+    """sha256 (first 16 hex digits) of the kernel sources (every csrc file but the
+    host-only pipeline wdm_api.cu), the key a traffic capture is valid for."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in sorted(os.listdir(CSRC)):
+        if f.endswith((".cu", ".cuh", ".h")) and f != "wdm_api.cu":
+            h.update(f.encode())
+            with open(os.path.join(CSRC, f), "rb") as fh:
+                h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def ncu_traffic(pass_name, n, workload, sched):
-    """Measured DRAM bytes per launch of the pass when the capture covers this run, else None."""
+    """(DRAM bytes per launch of the pass, provenance) from the committed capture,
+    or (None, reason) when the capture does not cover this run."""
     if n != 384 or workload != 3 or not sched:
-        return None
+        return None, "no capture of this workload"
+    if not os.path.exists(TRAFFIC_FILE):
+        return None, "no capture file"
+    with open(TRAFFIC_FILE) as f:
+        cap = json.load(f)
     impl = {"kick_xfft_fwd": "x_kick", "kick_final": "x_kick", "psi_z_drift": "psi_z", "psi_x_inv_rho": "x_rho_b",
             "rho_y_fwd": "h_y", "rho_z_poisson": "h_z", "phi_y_inv": "h_y"}.get(pass_name)
     if impl is None or impl not in sched:
-        return None
-    return NCU_TRAFFIC_384.get((pass_name, sched[impl]["impl"]))
+        return None, "pass not captured"
+    v = cap["passes"].get(f"{pass_name}/{sched[impl]['impl']}")
+    if v is None:
+        return None, "pass and implementation not captured"
+    same = cap.get("kernel_source_hash") == kernel_source_hash()
+    return v, {"capture": os.path.relpath(TRAFFIC_FILE, ROOT), "command": cap.get("command"),
+               "kernels_unchanged_since_capture": same}
+
+
+def free_port():
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_ranks(argv, n):
+    """Run this script again as n ranks on this node, one process per GPU, the
+    way the torchrun launch does; returns the launcher's exit status."""
+    # the launcher's own parser would take an abbreviation such as --n for one of its options
+    argv = ["--grid" + a[3:] if a == "--n" or a.startswith("--n=") else a for a in argv]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.abspath(__file__), *argv]
+    return subprocess.call(cmd)
 
 
 def measured_peaks():
@@ -146,6 +181,15 @@ def max_over_ranks(x, world):
 def replica_throughput(steps, world, seconds):
     """Whole-job steps/s of `world` replicas that each ran `steps` steps in `seconds` (the max over ranks)."""
     return steps * world / seconds
+
+
+def workload_config(wl, args, world):
+    """The config object of a bench line (the same for both arms)."""
+    N = wl["n"]
+    return {"workload": wl["name"], "grid": [N, N, N], "box": wl["L"], "dt": wl["dt"], "mode": args.mode,
+            "phase_mode": args.phase, "tidal": wl["tidal"] is not None,
+            "baryon_particles": 0 if wl["particles"] is None else len(wl["particles"][1]),
+            "l2": "inputs larger than L2 (psi 8 B/cell)", "parallelism": f"replicas x{world}"}
 
 
 def setup_context(wdm, wl, phase_mode, steps_total):
@@ -273,6 +317,7 @@ def run_native(args, rank, world):
                   "GBps": round(v["bytes_per_launch"] / (v["ms"] / max(v["launches"], 1) / 1e3) / 1e9, 1)}
               for k, v in prof.items() if v["launches"]}
     ncell = N ** 3
+    traffic, traffic_src = ncu_traffic(name, N, args.workload, sched)
     rec = {
         "metric": f"KDK steps/s at {N}^3 (Strang, complex FP32 psi, {args.phase} phases)",
         "value": round(value, 3),
@@ -286,13 +331,10 @@ def run_native(args, rank, world):
         "vs_baseline": None,
         "dtype": "c64",
         "data": "synthetic (seeded soliton + 4096-plane-wave NFW halo; Hernquist tide; 1e5 Plummer baryons)",
-        "config": {"workload": wl["name"], "grid": [N, N, N], "box": wl["L"], "dt": dt, "mode": args.mode,
-                   "phase_mode": args.phase, "tidal": wl["tidal"] is not None,
-                   "baryon_particles": 0 if wl["particles"] is None else len(wl["particles"][1]),
-                   "l2": "inputs larger than L2 (psi 8 B/cell)", "parallelism": f"replicas x{world}"},
+        "config": workload_config(wl, args, world),
         "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": ncu_traffic(name, N, args.workload, sched),
+                     "traffic": traffic, "traffic_source": traffic_src,
                      "bytes_per_launch": p["bytes_per_launch"], "mean_launch_ms": round(mean_ms, 5)},
         "step_effective": {"B_alg_per_cell": B_ALG_PER_CELL,
                            "GBps": round(B_ALG_PER_CELL * ncell * value / world / 1e9, 1),
@@ -477,24 +519,19 @@ def time_oracle_loop(wl, budget_s):
     return n / (time.perf_counter() - t0), n, spe.WORKERS
 
 
-def run_adjoint(args, rank, world):
-    """Workload 5: adjoint of 200 Strang steps at 128^3 (checkpoints every 20) vs the forward run."""
+def adjoint_part(wdm, phase, N=128, nsteps=200, ck=20, reps=1):
+    """Workload 5: adjoint of nsteps Strang steps at N^3 (checkpoints every ck) against the forward run."""
     import torch
 
-    import wavedm_gb300 as wdm
-
-    wdm.build_library()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     ics = wdm.ics
-    N, L = args.n or 128, 20.0
-    nsteps, ck = 200, 20
+    L = 20.0
     dt = ics.dt_for(N, L)
     D = np.array([2.0, -1.0, -1.0, 0.0, 0.0, 0.0])
     amp, rc = 0.02, 1.2
     psi0 = ics.soliton_halo_ic((N, N, N), (L, L, L), rc=rc, rng=ics.rng_for(5)).astype(np.complex64)
     target = (np.abs(ics.soliton_halo_ic((N, N, N), (L, L, L), rc=1.1 * rc, rng=ics.rng_for(5))) ** 2
               ).astype(np.float32)
-    ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=1.0, phase_mode=args.phase)
+    ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=1.0, phase_mode=phase)
     ctx.set_psi(psi0)
     ctx.set_tidal([amp * D])
     rho_d = torch.from_numpy(target).cuda()
@@ -504,7 +541,6 @@ def run_adjoint(args, rank, world):
     ctx.set_psi(psi0)
     ctx.adjoint(nsteps, dt, rho_d, ckpt_every=ck, tidal_dir=D, grad_out=grad_d)
     torch.cuda.synchronize()
-    reps = max(1, args.steps // 10)
     t0 = time.perf_counter()
     for _ in range(reps):
         ctx.set_psi(psi0)
@@ -524,17 +560,96 @@ def run_adjoint(args, rank, world):
     prof = {k: {"launches": v["launches"], "ms": round(v["ms"], 3)} for k, v in ctx.profile().items() if v["launches"]}
     ctx.set_profiling(False)
     ctx.close()
+    return {"ratio": round(t_adj / t_fwd, 3), "grid": [N, N, N], "steps": nsteps, "ckpt_every": ck, "dt": dt,
+            "repeats": reps, "forward_steps_per_s": round(nsteps / t_fwd, 2),
+            "adjoint_steps_per_s": round(nsteps / t_adj, 2), "loss": float(loss), "dL_damp": float(da),
+            "gpu_launches": int(launches), "passes_adjoint_run": prof,
+            "timing": "host wall clock around synchronous calls, whole runs (forward: set_psi + wdm_step of all "
+                      "steps; adjoint: set_psi + wdm_adjoint)"}
+
+
+def run_adjoint(args, rank, world):
+    """Workload 5 as its own bench line: the adjoint/forward time ratio."""
+    import torch
+
+    import wavedm_gb300 as wdm
+
+    wdm.build_library()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    a = adjoint_part(wdm, args.phase, N=args.n or 128, reps=max(1, args.steps // 10))
+    N, nsteps, ck = a["grid"][0], a["steps"], a["ckpt_every"]
     return {
-        "passes_adjoint_run": prof,
+        "passes_adjoint_run": a["passes_adjoint_run"],
         "metric": f"adjoint/forward time ratio, {nsteps} Strang steps at {N}^3, checkpoints every {ck}",
-        "value": round(t_adj / t_fwd, 3), "unit": "ratio", "n_gpus": world, "steps": nsteps, "warmup": nsteps,
-        "ms_per_step": round(t_adj / nsteps * 1e3, 4), "higher_is_better": False, "scaling": "weak",
+        "value": a["ratio"], "unit": "ratio", "n_gpus": world, "steps": nsteps, "warmup": nsteps,
+        "ms_per_step": round(1e3 / a["adjoint_steps_per_s"], 4), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded soliton + halo; target from rc x 1.1)",
-        "config": {"workload": "adjoint128", "grid": [N, N, N], "dt": dt, "ckpt_every": ck, "repeats": reps,
-                   "phase_mode": args.phase},
-        "forward_steps_per_s": round(nsteps / t_fwd, 2), "adjoint_steps_per_s": round(nsteps / t_adj, 2),
-        "loss": float(loss), "dL_damp": float(da), "gpu_launches": int(launches),
+        "config": {"workload": "adjoint128", "grid": a["grid"], "dt": a["dt"], "ckpt_every": ck,
+                   "repeats": a["repeats"], "phase_mode": args.phase},
+        "forward_steps_per_s": a["forward_steps_per_s"], "adjoint_steps_per_s": a["adjoint_steps_per_s"],
+        "loss": a["loss"], "dL_damp": a["dL_damp"], "gpu_launches": a["gpu_launches"],
     }
+
+
+def plain_part(wdm, wl, K, W, mode):
+    """steps/s of the plain FP32 phase form on the same workload, timed like `value`."""
+    import torch
+
+    dt = wl["dt"]
+    ctx, psi0 = setup_context(wdm, wl, "plain", max(K, W, 1))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.step(W, dt, mode=mode)
+    ctx.set_psi(psi0)
+    ctx.get_phi()
+    if wl["tidal"] is not None:
+        ctx.set_tidal(wl["tidal"](np.arange(K + 1) * dt))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    ctx.step(K, dt, mode=mode, sync=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    ok = ctx.is_finite()
+    ctx.close()
+    return {"value": round(K / (ms / 1e3), 3), "unit": "steps/s", "steps": K, "ms_per_step": round(ms / K, 4),
+            "phase_mode": "plain", "finite": bool(ok)}
+
+
+def accuracy_part(wdm, wl, oracle_steps, mass_steps):
+    """psi and rho rel-L2 against the FP64 oracle after oracle_steps Strang steps of
+    the workload (precise and plain phase forms), and the relative mass drift of
+    both forms over mass_steps steps (GPU only: the FP64 path conserves mass to
+    ~1e-13, so the drift needs no reference run)."""
+    from oracle import spe
+
+    N, L, dt = wl["n"], wl["L"], wl["dt"]
+    psi0 = wl["psi0"].astype(np.complex64)
+    spe_, g, phys = oracle_setup(wl, oracle_steps)
+    t0 = time.perf_counter()
+    ref = spe.run(psi0.astype(np.complex128), g, phys, dt, oracle_steps)
+    t_oracle = time.perf_counter() - t0
+    rho_ref = np.abs(ref) ** 2
+    out = {"oracle_steps": oracle_steps, "oracle_seconds": round(t_oracle, 1), "oracle_threads": spe.WORKERS,
+           "tolerance_psi_rel_l2": 1e-5, "mass_steps": mass_steps, "tolerance_mass_drift": 1e-6}
+    rows = wl["tidal"](np.arange(mass_steps + 1) * dt) if wl["tidal"] is not None else None
+    for mode in ("precise", "plain"):
+        ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=wl["poisson_coeff"], phase_mode=mode)
+        ctx.set_psi(psi0)
+        if rows is not None:
+            ctx.set_tidal(rows, t_first=0.0, t_step=dt)
+        if wl["particles"] is not None:
+            ctx.set_particles(*wl["particles"])
+        m0 = ctx.reduce()["mass"]
+        ctx.step(oracle_steps, dt, t0=0.0)
+        psi = ctx.get_psi()
+        r = {"psi_rel_l2": spe.rel_l2(psi, ref), "rho_rel_l2": spe.rel_l2(np.abs(psi) ** 2, rho_ref)}
+        ctx.step(mass_steps - oracle_steps, dt, t0=oracle_steps * dt)
+        r["mass_drift"] = float(ctx.reduce()["mass"] / m0 - 1.0)
+        ctx.close()
+        out[mode] = r
+    out["pass"] = bool(out["precise"]["psi_rel_l2"] <= 1e-5 and abs(out["precise"]["mass_drift"]) <= 1e-6)
+    return out
 
 
 def ensemble_cpu_baseline(budget_s):
@@ -570,17 +685,28 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--workload", type=int, default=3)
-    ap.add_argument("--n", type=int, default=None, help="override the grid size of the workload")
+    ap.add_argument("--grid", "--n", dest="n", type=int, default=None, help="override the grid size of the workload")
     ap.add_argument("--phase", choices=["precise", "plain"], default="precise")
     ap.add_argument("--mode", choices=["strang", "reference_loop", "lie"], default="strang")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of oracle time for cpu_baseline")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave out the metric's other parts (accuracy vs the FP64 oracle, mass drift over the "
+                         "workload's steps, the plain phase form, the adjoint ratio, the ensemble)")
+    ap.add_argument("--acc-steps", type=int, default=10, help="Strang steps of the accuracy check against the oracle")
+    ap.add_argument("--mass-steps", type=int, default=None, help="steps of the mass-drift check (default: the "
+                                                                   "workload's own step count)")
     args = ap.parse_args()
 
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        # one process per GPU, launched here the way torchrun launches them
+        sys.exit(launch_ranks(sys.argv[1:], args.gpus))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if world != args.gpus:
+        raise SystemExit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}")
 
     if args.impl == "reference":
         if rank != 0:
@@ -597,7 +723,7 @@ def main():
             "value": round(v, 5), "unit": "steps/s", "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1),
             "ms_per_step": round(1e3 / v, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c128", "data": "synthetic (same seeded workload)",
-            "config": {"workload": wl["name"], "grid": [N, N, N], "mode": "strang"},
+            "config": workload_config(wl, args, args.gpus),
             "cpu_baseline": {"value": round(v, 5), "unit": "steps/s", "cores": cores, "kind": "port",
                              "sample": sample,
                              "what": "oracle/spe.py: numpy/scipy.fft FP64 restatement of the reference's FFTW "
@@ -632,6 +758,22 @@ def main():
             print(json.dumps(rec), flush=True)
         return
     rec = run_native(args, rank, world)
+    if rank == 0 and not args.no_extras and args.workload == 3:
+        # the rest of the metric: accuracy at the stated tolerance, the plain
+        # FP32 form beside the precise one, the adjoint/forward ratio, the ensemble
+        import copy
+
+        import wavedm_gb300 as wdm
+
+        wl = wdm.ics.workload(args.workload, n=args.n)
+        rec["plain"] = plain_part(wdm, wl, args.steps, args.warmup, args.mode)
+        rec["accuracy"] = accuracy_part(wdm, wl, args.acc_steps, args.mass_steps or wl["steps"])
+        rec["adjoint"] = adjoint_part(wdm, args.phase)
+        ea = copy.copy(args)
+        ea.no_e2e, ea.n = True, None
+        e = run_ensemble(ea, 0, 1)
+        rec["ensemble"] = {k: e[k] for k in ("metric", "value", "unit", "steps", "ms_per_step", "halo_steps_per_s",
+                                             "gpu_launches", "config", "roofline")}
     if rank == 0 and not args.no_cpu_baseline:
         import wavedm_gb300 as wdm
 

@@ -95,21 +95,37 @@ wdm_status wdm_get_rho(wdm_ctx* ctx, float* rho, int32_t where);
 wdm_status wdm_get_phi(wdm_ctx* ctx, float* phi, int32_t where);
 /* static external potential V [batch][nz][ny][nx] float32; NULL clears it */
 wdm_status wdm_set_static_potential(wdm_ctx* ctx, const float* V, int32_t where);
-/* tidal tensor 1/2 x^T T x about the box centre, T = (xx, yy, zz, xy, xz, yz).
- * schedule: nsched rows of 6 doubles, row s used by the kick at time t0 + s*dt of
- * the next wdm_step (a row per batch item when nsched == batch and per_item != 0).
- * nsched == 0 turns the tide off. */
+/* tidal tensor 1/2 x^T T x about the box centre, T = (xx, yy, zz, xy, xz, yz),
+ * replacing the tide add_tidal_potential! evaluates at time t[i]
+ * (src/physics/tidal_fields.jl:64-118).
+ * schedule: nsched rows of 6 doubles.  Without a clock (the state after this
+ * call) row s is used by kick s of every following wdm_step call, the kick at
+ * time t0 + s*dt, whatever t0 is; a single row is a constant tide.
+ * per_item != 0: one constant row per batch item (nsched == batch).
+ * nsched == 0 turns the tide off.  Either form clears the clock. */
 wdm_status wdm_set_tidal(wdm_ctx* ctx, const double* schedule, int32_t nsched, int32_t per_item);
+/* Gives the shared-row schedule of wdm_set_tidal a clock: row s is the tensor
+ * at time t_first + s*t_step.  Every kick then uses the row nearest to its own
+ * time (wdm_step: t0 + s*dt; wdm_kick: t; wdm_adjoint: s*dt from t = 0), and a
+ * call whose kicks fall outside the rows returns WDM_ERR_INVALID.  t_step == 0
+ * removes the clock.  A clocked schedule of several rows cannot be replayed by
+ * wdm_step_graph or a group (their graphs do not follow the time):
+ * WDM_ERR_STATE.  No counterpart in the reference, whose tide is a function
+ * of t evaluated on the host every step. */
+wdm_status wdm_set_tidal_clock(wdm_ctx* ctx, double t_first, double t_step);
 /* baryon particles (positions [n][3] and masses [n], doubles), CIC-deposited
  * into the density before every Poisson solve; n == 0 removes them. */
 wdm_status wdm_set_particles(wdm_ctx* ctx, const double* pos, const double* mass, int64_t n);
 
 /* the path ------------------------------------------------------------------ */
-/* nsteps steps of size dt from time t0 */
+/* nsteps steps of size dt from time t0: kick s runs at time t0 + s*dt (the
+ * Strang step's closing half kick is kick nsteps), which selects its tidal
+ * row when the schedule has a clock (wdm_set_tidal_clock) */
 wdm_status wdm_step(wdm_ctx* ctx, int32_t nsteps, double dt, double t0, int32_t mode);
 wdm_status wdm_step_async(wdm_ctx* ctx, int32_t nsteps, double dt, double t0, int32_t mode);
 /* wdm_step through a CUDA graph: the launches of nsteps steps are captured once
- * per (nsteps, dt, mode, state) and replayed; returns when the steps are done. */
+ * per (nsteps, dt, mode, state) and replayed; returns when the steps are done.
+ * Every replay uses tidal rows 0..nsteps of an unclocked schedule. */
 wdm_status wdm_step_graph(wdm_ctx* ctx, int32_t nsteps, double dt, int32_t mode);
 
 /* ensembles: contexts of different grid sizes (each holding `batch` halos of
@@ -129,7 +145,9 @@ void* wdm_group_stream(const wdm_group* g);
 /* kernel launches executed by the group's graph replays so far */
 int64_t wdm_group_launch_count(const wdm_group* g);
 
-/* apply_kick_step!: Phi from |psi|^2, psi <- exp(-i dt (Phi + V + tide(t))) psi */
+/* apply_kick_step!: Phi from |psi|^2, psi <- exp(-i dt (Phi + V + tide(t))) psi.
+ * tide(t) is the clocked schedule's row nearest to t, or the single row of a
+ * constant tide; an unclocked schedule of several rows gives WDM_ERR_STATE. */
 wdm_status wdm_kick(wdm_ctx* ctx, double dt, double t);
 /* apply_drift_step!: psi <- mask * ifft(exp(-i k^2 dt/2) fft(psi)) */
 wdm_status wdm_drift(wdm_ctx* ctx, double dt);
@@ -148,10 +166,15 @@ wdm_status wdm_fft3d(wdm_ctx* ctx, void* data_dev, int32_t dir);
  * GPU loading the library holds until the process exits; grids are limited to
  * (nx/2+1)*ny*nz <= 1,064,960 (a 128^3 grid), larger ones return
  * WDM_ERR_INVALID.  rho and phi are float32 device pointers [nz][ny][nx]; stream is
- * a cudaStream_t (NULL: the default stream); the call returns when phi is ready.
+ * a cudaStream_t (NULL: the default stream).  The call synchronises that stream
+ * before it returns, so phi is ready on return.
  * The first call on a device looks up the array's device address once, so make
  * that first call before any stream capture.  All calls share the array: calls
  * whose work overlaps on the GPU race and must be serialised by the caller.
+ * It builds its twiddle tables on the device (FP64 sincospi) where wdm_poisson
+ * builds them on the host, and it always takes the register-tile line passes
+ * and the direct x passes, so its phi agrees with wdm_poisson's to FP32
+ * rounding, not bit for bit.
  * Errors are reported through wdm_last_error(NULL).
  * No counterpart in the reference: it is an addition of this library. */
 wdm_status wdm_poisson_noalloc(const float* rho_dev, float* phi_dev, int32_t nx, int32_t ny, int32_t nz,

@@ -115,18 +115,54 @@ def test_step_matches_golden(wdm, path, phase_mode):
     assert spe.rel_l2(phi, d["phi"]) < 2e-5
 
 
-@pytest.mark.parametrize("path", GOLDEN[:2], ids=[os.path.basename(f)[:-4] for f in GOLDEN[:2]])
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(f)[:-4] for f in GOLDEN])
 def test_step_in_pieces_equals_one_call(wdm, path):
-    """Several wdm_step calls chain like one (the potential stays valid across calls)."""
+    """Several wdm_step calls chain like one (the potential stays valid across
+    calls); a time-dependent tide follows t0 through the schedule's clock."""
     d = dict(np.load(path))
-    if "tidal" in d:
-        pytest.skip("schedule rows are per call")
     steps, dt = int(d["steps"]), float(d["dt"])
     with _ctx_for_golden(wdm, d) as ctx:
+        if "tidal" in d:
+            ctx.set_tidal(d["tidal"], t_first=0.0, t_step=dt)
         for s in range(steps):
             ctx.step(1, dt, t0=s * dt, mode=str(d["mode"]))
         psi = ctx.get_psi()
     assert spe.rel_l2(psi, d["psi"]) < 2e-5
+    # the same pieces bit for bit as one call over the clocked schedule
+    with _ctx_for_golden(wdm, d) as ctx:
+        if "tidal" in d:
+            ctx.set_tidal(d["tidal"], t_first=0.0, t_step=dt)
+        ctx.step(steps, dt, t0=0.0, mode=str(d["mode"]))
+        one = ctx.get_psi()
+    assert np.array_equal(psi, one)
+
+
+def test_kick_follows_the_tidal_clock(wdm):
+    """wdm_kick(dt, t) takes the clocked row nearest to t; without a clock a
+    schedule of several rows is refused rather than read at a frozen row."""
+    d = dict(np.load(os.path.join(HERE, "golden", "lie_12x16x8_tidal.npz")))
+    rows, dt = d["tidal"], float(d["dt"])
+    with _ctx_for_golden(wdm, d) as ctx:
+        with pytest.raises(wdm._abi.WdmError, match="WDM_ERR_STATE"):
+            ctx.kick(dt, 0.0)
+        ctx.set_tidal(rows, t_first=1.0, t_step=dt)
+        ctx.kick(dt, 1.0 + 3 * dt + 0.2 * dt)  # nearest row: 3
+        got = ctx.get_psi()
+        with pytest.raises(wdm._abi.WdmError, match="WDM_ERR_INVALID"):
+            ctx.kick(dt, 1.0 - dt)  # before the first row
+    with _ctx_for_golden(wdm, d) as ctx:
+        ctx.set_tidal(rows[3:4])
+        ctx.kick(dt, 123.0)  # a constant tide: any time
+        ref = ctx.get_psi()
+    assert np.array_equal(got, ref)
+    n = tuple(int(v) for v in d["n"])
+    with wdm.SPEContext(n, tuple(float(v) for v in d["L"])) as ctx:
+        ctx.set_psi(d["psi0"])
+        ctx.set_tidal(rows, t_first=0.0, t_step=dt)
+        with pytest.raises(wdm._abi.WdmError, match="WDM_ERR_STATE"):
+            ctx.step_graph(2, dt)
+        with pytest.raises(wdm._abi.WdmError, match="WDM_ERR_INVALID"):
+            ctx.step(6, dt, t0=0.0)  # kicks up to t = 6 dt, rows end at 5 dt
 
 
 def test_kick_and_drift_match_oracle(wdm):

@@ -78,3 +78,28 @@ def test_reference_arm_prints_on_rank0_only(rank):
         assert d["cpu_baseline"]["kind"] == "port"
     else:
         assert lines == []
+
+
+def test_gpus_flag_launches_one_process_per_rank():
+    """`bench.py --gpus 2` started as one process spawns its two ranks itself (as
+    torchrun would): exactly one JSON line comes back, from rank 0, and it
+    reports two GPUs.  The reference arm needs no GPU, so this runs on CPU."""
+    pytest.importorskip("torch")
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR",
+                                                           "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--workload", "1", "--n", "16", "--steps", "2", "--warmup", "1"],
+                       env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2
+
+
+def test_world_size_must_match_gpus_flag():
+    env = dict(os.environ, RANK="0", WORLD_SIZE="2", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "4",
+                        "--workload", "1", "--n", "16", "--steps", "1", "--warmup", "1"],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode != 0 and "WORLD_SIZE=2" in r.stderr

@@ -4,9 +4,10 @@ wdm_poisson_noalloc serves callers that cannot allocate device memory (a host
 runtime that owns the GPU memory pool, or a loop that must not pay for the
 device synchronisation of cudaMalloc/cudaFree): its scratch is a static device
 array, so it must agree with the context-based wdm_poisson, which allocates its
-own scratch.  Two calls in a row check that nothing left in the shared array
-by one call leaks into the next.  This file is collected last so that a run
-stopping at the first failure has already run every other test.
+own scratch.  Calls in a row check that nothing left in the shared array by
+one call leaks into the next: the same input solved again after a call on
+another grid shape must give the same bits.  This file is collected last so
+that a run stopping at the first failure has already run every other test.
 """
 import ctypes as C
 
@@ -36,6 +37,7 @@ def test_noalloc_poisson_matches_wdm_poisson_twice(wdm, torch_cuda):
     torch = torch_cuda
     lib = wdm._abi.load()
     cases = [((32, 48, 24), (3.0, 2.0, 4.0), 4 * np.pi, 11), ((64, 64, 64), (20.0, 20.0, 20.0), 1.0, 12)]
+    results = []
     for n, L, coeff, seed in cases:
         nx, ny, nz = n
         rng = np.random.default_rng(seed)
@@ -50,6 +52,17 @@ def test_noalloc_poisson_matches_wdm_poisson_twice(wdm, torch_cuda):
         assert np.all(np.isfinite(got))
         # same kernels on the same data: the test_gpu_parity Poisson tolerance
         assert spe.rel_l2(got, ref) < 2e-6
+        # and the FP64 oracle's solve of the same density (white noise: the
+        # tolerance of test_poisson_matches_oracle)
+        oracle = spe.poisson(rho_h.astype(np.float64), spe.Grid(n, L), coeff)
+        assert spe.rel_l2(got, oracle) < 4e-6
+        results.append((n, L, coeff, rho, got))
+    # Solve the first case again, now that the second (larger) case has filled
+    # the shared array: bit for bit the first answer.
+    n, L, coeff, rho, first = results[0]
+    again = torch.full_like(rho, float("nan"))
+    assert _noalloc(lib, rho, again, n, L, coeff) == 0, lib.wdm_last_error(None)
+    assert np.array_equal(again.cpu().numpy(), first)
 
 
 def test_noalloc_rejects_grids_beyond_the_static_scratch(wdm, torch_cuda):

@@ -57,6 +57,7 @@ SIGNATURES = [
     ("wdm_get_phi", _i32, [_vp, _vp, _i32]),
     ("wdm_set_static_potential", _i32, [_vp, _vp, _i32]),
     ("wdm_set_tidal", _i32, [_vp, _vp, _i32, _i32]),
+    ("wdm_set_tidal_clock", _i32, [_vp, _d, _d]),
     ("wdm_set_particles", _i32, [_vp, _vp, _vp, _i64]),
     ("wdm_step", _i32, [_vp, _i32, _d, _d, _i32]),
     ("wdm_step_async", _i32, [_vp, _i32, _d, _d, _i32]),

@@ -119,14 +119,21 @@ class SPEContext:
         p, w = _ptr(V)
         self._check(self.lib.wdm_set_static_potential(self.handle, p, w))
 
-    def set_tidal(self, schedule, per_item=False):
-        """Rows of (Txx, Tyy, Tzz, Txy, Txz, Tyz): row s is used by the s-th kick of the next step call."""
+    def set_tidal(self, schedule, per_item=False, t_first=None, t_step=None):
+        """Rows of (Txx, Tyy, Tzz, Txy, Txz, Tyz).
+
+        Without ``t_step`` row s is used by the s-th kick of every following
+        step call.  With ``t_step`` (and ``t_first``, default 0) row s is the
+        tensor at time t_first + s t_step and each kick takes the row nearest
+        to its own time (step's t0 + s dt, kick's t)."""
         if schedule is None:
             self._check(self.lib.wdm_set_tidal(self.handle, None, 0, 0))
             return
         s = np.ascontiguousarray(np.asarray(schedule, dtype=np.float64).reshape(-1, 6))
         self._tidal_keep = s
         self._check(self.lib.wdm_set_tidal(self.handle, C.c_void_p(s.ctypes.data), len(s), int(per_item)))
+        if t_step is not None:
+            self._check(self.lib.wdm_set_tidal_clock(self.handle, float(t_first or 0.0), float(t_step)))
 
     def set_particles(self, pos, mass):
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)

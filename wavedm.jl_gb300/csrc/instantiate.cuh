@@ -1,39 +1,64 @@
 // Launchers of the pass kernels for one axis length N (included by sizes_*.cu).
 #pragma once
+#include <atomic>
 #include <cmath>
 #include "kernel_set.h"
 #include "xpass_warp.cuh"
 
 namespace wdm {
 
-// Opt a kernel in to more than 48 KB of dynamic shared memory, once per process.
+// Launch settings are device properties: each is found once per device (the
+// current one at the launch) and kept in a slot per device ordinal.
+constexpr int MAX_DEVICES = 64;
+
+static int current_device() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return dev >= 0 && dev < MAX_DEVICES ? dev : 0;
+}
+
+// Opt a kernel in to more than 48 KB of dynamic shared memory, once per device.
 template <auto K>
 static cudaError_t prep_once(size_t smem) {
-  static const cudaError_t e =
-      smem > 48 * 1024 ? cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) : cudaSuccess;
-  return e;
+  if (smem <= 48 * 1024) return cudaSuccess;
+  // 0: not yet, 1: done, 2 + e: failed with cudaError_t e
+  static std::atomic<int> state[MAX_DEVICES];
+  std::atomic<int>& st = state[current_device()];
+  int v = st.load(std::memory_order_acquire);
+  if (v == 0) {
+    const cudaError_t e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    v = e == cudaSuccess ? 1 : 2 + (int)e;
+    st.store(v, std::memory_order_release);
+  }
+  return v == 1 ? cudaSuccess : (cudaError_t)(v - 2);
 }
 
-// SMs of the current device (queried once).
+// SMs of the current device.
 static int sm_count() {
-  static const int n = [] {
-    int dev = 0, v = 0;
-    cudaGetDevice(&dev);
+  static std::atomic<int> n[MAX_DEVICES];
+  const int dev = current_device();
+  int v = n[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    return v > 0 ? v : 1;
-  }();
-  return n;
+    v = v > 0 ? v : 1;
+    n[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
 }
 
-// Resident CTAs per SM of a kernel at its block size and shared memory (once).
+// Resident CTAs per SM of a kernel at its block size and shared memory, on the
+// current device (each call site passes one fixed size).
 template <auto K>
 static int resident_ctas(int threads, size_t smem) {
-  static const int n = [&] {
-    int v = 0;
+  static std::atomic<int> n[MAX_DEVICES];
+  std::atomic<int>& slot = n[current_device()];
+  int v = slot.load(std::memory_order_relaxed);
+  if (v == 0) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, K, threads, smem);
-    return v > 0 ? v : 1;
-  }();
-  return n;
+    v = v > 0 ? v : 1;
+    slot.store(v, std::memory_order_relaxed);
+  }
+  return v;
 }
 
 template <int N>

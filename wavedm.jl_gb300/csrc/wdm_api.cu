@@ -133,6 +133,9 @@ struct wdm_ctx {
   float* T6b = nullptr;             // per-batch-item tidal tensors
   std::vector<double> tide;         // host schedule rows of 6
   int tide_on = 0;
+  // clock of the schedule: row s is the tensor at time tide_t0 + s tide_dt
+  // (tide_dt == 0: no clock, row s belongs to kick s of each wdm_step call)
+  double tide_t0 = 0.0, tide_dt = 0.0;
   int* flag = nullptr;              // device words: [0] non-finite psi, [1] abandoned-wait bits
   float* scratch_f = nullptr;       // float field scratch [batch][ncell]
   float2* scratch_h = nullptr;      // half-spectrum scratch
@@ -269,14 +272,40 @@ static wdm_status cuda_fail(wdm_ctx* c, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail((c), e_, #call); \
   } while (0)
 
+// Host-side fault injection (no GPU fault): WDM_FAULT=nonfinite makes the
+// finite check report a non-finite density; WDM_FAULT=alloc makes every device
+// allocation fail, and WDM_FAULT=alloc:N only the N-th one counted since the
+// variable took its present value (so a context creation can fail half way).
 static bool fault_injected(const char* what) {
   const char* f = std::getenv("WDM_FAULT");
   return f && std::strstr(f, what) != nullptr;
 }
 
+static std::mutex g_fault_mu;
+static std::string g_fault_value;
+static long long g_fault_allocs = 0;
+
+static bool alloc_fault_injected() {
+  const char* f = std::getenv("WDM_FAULT");
+  if (!f) return false;
+  const char* a = std::strstr(f, "alloc");
+  if (!a) return false;
+  std::lock_guard<std::mutex> lock(g_fault_mu);
+  if (g_fault_value != f) {
+    g_fault_value = f;
+    g_fault_allocs = 0;
+  }
+  ++g_fault_allocs;
+  if (a[5] != ':') return true;
+  return g_fault_allocs == std::atoll(a + 6);
+}
+
 template <class T>
 static wdm_status dalloc(wdm_ctx* c, T** p, size_t count) {
-  if (fault_injected("alloc")) return fail(c, WDM_ERR_ALLOC, "injected allocation failure (WDM_FAULT=alloc)");
+  if (alloc_fault_injected()) {
+    *p = nullptr;
+    return fail(c, WDM_ERR_ALLOC, "injected allocation failure (WDM_FAULT=alloc)");
+  }
   cudaError_t e = cudaMalloc((void**)p, count * sizeof(T) + 16);
   if (e != cudaSuccess) {
     *p = nullptr;
@@ -532,6 +561,35 @@ static KickArgs kick_args(const wdm_ctx* c, double dt, int sched_row) {
   a.precise = c->d.phase_mode == WDM_PHASE_PRECISE;
   a.err = c->flag + 1;
   return a;
+}
+
+// Schedule row of the kick at time t that is kick s of a call: with a clock
+// the row whose time is nearest to t, without one row s.  A one-row schedule
+// is a constant tide (row 0 at every time).
+static int tide_row(const wdm_ctx* c, double t, int s) {
+  if (c->tide.size() <= 6) return 0;
+  if (c->tide_dt > 0.0) return (int)std::floor((t - c->tide_t0) / c->tide_dt + 0.5);
+  return s;
+}
+
+// The kicks at times t0 + s dt, s = 0 .. nkicks-1, of one call all have a row.
+static wdm_status check_tide_rows(wdm_ctx* c, double t0, double dt, int nkicks, const char* who) {
+  if (c->tide_on != 1 || nkicks <= 0) return WDM_OK;
+  const int nrow = (int)(c->tide.size() / 6);
+  if (nrow == 1) return WDM_OK;
+  for (int s : {0, nkicks - 1}) {
+    const int r = tide_row(c, t0 + s * dt, s);
+    if (r < 0 || r >= nrow) {
+      if (c->tide_dt > 0.0)
+        return fail(c, WDM_ERR_INVALID, std::string(who) + ": the kick at t = " + std::to_string(t0 + s * dt) +
+                                            " falls outside the tidal schedule (" + std::to_string(nrow) +
+                                            " rows from t = " + std::to_string(c->tide_t0) + " every " +
+                                            std::to_string(c->tide_dt) + ")");
+      return fail(c, WDM_ERR_INVALID, std::string(who) + ": tidal schedule has " + std::to_string(nrow) +
+                                          " rows, the call needs " + std::to_string(nkicks) + " (or exactly 1)");
+    }
+  }
+  return WDM_OK;
 }
 
 // Kick of psi (in place), or of psi_in into c->psi when psi_in is given.
@@ -965,6 +1023,8 @@ wdm_status wdm_set_tidal(wdm_ctx* c, const double* sched, int32_t nsched, int32_
   if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
   c->version++;
   if (nsched < 0) return fail(c, WDM_ERR_INVALID, "nsched < 0");
+  c->tide_t0 = 0.0;
+  c->tide_dt = 0.0;
   if (nsched == 0) {
     c->tide_on = 0;
     c->tide.clear();
@@ -983,6 +1043,18 @@ wdm_status wdm_set_tidal(wdm_ctx* c, const double* sched, int32_t nsched, int32_
     c->tide.assign(sched, sched + (size_t)6 * nsched);
     c->tide_on = 1;
   }
+  return WDM_OK;
+}
+
+wdm_status wdm_set_tidal_clock(wdm_ctx* c, double t_first, double t_step) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (!std::isfinite(t_first) || !std::isfinite(t_step) || t_step < 0.0)
+    return fail(c, WDM_ERR_INVALID, "wdm_set_tidal_clock: t_first must be finite and t_step finite and >= 0");
+  if (c->tide_on != 1 && t_step > 0.0)
+    return fail(c, WDM_ERR_STATE, "wdm_set_tidal_clock: set a schedule of shared rows with wdm_set_tidal first");
+  c->version++;
+  c->tide_t0 = t_first;
+  c->tide_dt = t_step;
   return WDM_OK;
 }
 
@@ -1047,26 +1119,21 @@ static wdm_status step_impl(wdm_ctx* c, int32_t nsteps, double dt, double t0, in
   if (!(std::isfinite(dt))) return fail(c, WDM_ERR_INVALID, "dt is not finite");
   if (mode != WDM_STEP_STRANG && mode != WDM_STEP_REFERENCE_LOOP && mode != WDM_STEP_LIE)
     return fail(c, WDM_ERR_INVALID, "unknown step mode");
-  if (c->tide_on == 1) {
-    const size_t need = (size_t)nsteps + 1;
-    const size_t have = c->tide.size() / 6;
-    if (have != 1 && have < need)
-      return fail(c, WDM_ERR_INVALID, "tidal schedule has " + std::to_string(have) + " rows, the step needs " +
-                                          std::to_string(need) + " (or exactly 1)");
-  }
-  (void)t0;
+  if (!std::isfinite(t0)) return fail(c, WDM_ERR_INVALID, "t0 is not finite");
+  // kick s runs at time t0 + s dt (the Strang step's closing half kick is kick nsteps)
   if (nsteps == 0) return WDM_OK;
+  WDM_TRY(check_tide_rows(c, t0, dt, nsteps + 1, "wdm_step"));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
   for (int s = 0; s < nsteps; ++s) {
     double kdt;
     if (mode == WDM_STEP_STRANG) kdt = (s == 0) ? 0.5 * dt : dt;  // interior half kicks merged
     else if (mode == WDM_STEP_REFERENCE_LOOP) kdt = 0.5 * dt;
     else kdt = dt;
-    WDM_TRY(kick(c, kdt, s, true));
+    WDM_TRY(kick(c, kdt, tide_row(c, t0 + s * dt, s), true));
     WDM_TRY(drift_yz(c, dt));
     WDM_TRY(density_poisson(c, 1, dt));
   }
-  if (mode == WDM_STEP_STRANG) WDM_TRY(kick(c, 0.5 * dt, nsteps, false));
+  if (mode == WDM_STEP_STRANG) WDM_TRY(kick(c, 0.5 * dt, tide_row(c, t0 + nsteps * dt, nsteps), false));
   return WDM_OK;
 }
 
@@ -1081,9 +1148,14 @@ wdm_status wdm_step(wdm_ctx* c, int32_t nsteps, double dt, double t0, int32_t mo
 
 wdm_status wdm_kick(wdm_ctx* c, double dt, double t) {
   WDM_TRY(need_psi(c));
-  (void)t;
+  if (!std::isfinite(dt) || !std::isfinite(t)) return fail(c, WDM_ERR_INVALID, "wdm_kick: dt and t must be finite");
+  if (c->tide_on == 1 && c->tide.size() > 6 && !(c->tide_dt > 0.0))
+    return fail(c, WDM_ERR_STATE,
+                "wdm_kick: the tidal schedule has several rows but no clock (wdm_set_tidal_clock), so time t "
+                "selects no row");
+  WDM_TRY(check_tide_rows(c, t, 0.0, 1, "wdm_kick"));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, 0.0));
-  WDM_TRY(kick(c, dt, 0, false));
+  WDM_TRY(kick(c, dt, tide_row(c, t, 0), false));
   return sync_and_check(c);
 }
 
@@ -1514,7 +1586,7 @@ static wdm_status copy_pair(wdm_ctx* c, float2* dp, float2* dh, const float2* sp
 
 // one boundary of the forward run: kick of boundary b, drift, density and Poisson
 static wdm_status forward_boundary(wdm_ctx* c, int b, double dt) {
-  WDM_TRY(kick(c, b == 0 ? 0.5 * dt : dt, b, true));
+  WDM_TRY(kick(c, b == 0 ? 0.5 * dt : dt, tide_row(c, b * dt, b), true));
   WDM_TRY(drift_yz(c, dt));
   return density_poisson(c, 1, dt);
 }
@@ -1527,7 +1599,7 @@ static wdm_status forward_boundary_to(wdm_ctx* c, int b, double dt, const float2
   float2* keep_H = c->H;
   c->psi = psi_out;
   c->H = H_in;
-  wdm_status s = kick(c, b == 0 ? 0.5 * dt : dt, b, true, psi_in);
+  wdm_status s = kick(c, b == 0 ? 0.5 * dt : dt, tide_row(c, b * dt, b), true, psi_in);
   if (s == WDM_OK) s = drift_yz(c, dt);
   c->H = H_out;
   if (s == WDM_OK) s = density_poisson(c, 1, dt);
@@ -1541,11 +1613,7 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   WDM_TRY(need_psi(c));
   if (nsteps < 1 || ck < 1) return fail(c, WDM_ERR_INVALID, "wdm_adjoint: nsteps and ckpt_every must be >= 1");
   if (!rho_target || !grad || !loss) return fail(c, WDM_ERR_INVALID, "wdm_adjoint: null argument");
-  if (c->tide_on == 1) {
-    const size_t have = c->tide.size() / 6;
-    if (have != 1 && have < (size_t)nsteps + 1)
-      return fail(c, WDM_ERR_INVALID, "wdm_adjoint: tidal schedule needs nsteps+1 rows (or exactly 1)");
-  }
+  WDM_TRY(check_tide_rows(c, 0.0, dt, nsteps + 1, "wdm_adjoint"));
   const int B = c->d.batch;
   const size_t nc = (size_t)B * c->ncell, nh = (size_t)B * c->nhalf;
   if (!c->lam) WDM_TRY(dalloc(c, &c->lam, nc));
@@ -1604,7 +1672,7 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   {  // psi_N = final half kick of s_N, into the context's psi (psi_0 is kept in ck[0])
     float2* keep_H = c->H;
     c->H = st_H(last_seg, nsteps);
-    wdm_status s = kick(c, 0.5 * dt, nsteps, false, st_psi(last_seg, nsteps));
+    wdm_status s = kick(c, 0.5 * dt, tide_row(c, nsteps * dt, nsteps), false, st_psi(last_seg, nsteps));
     c->H = keep_H;
     WDM_TRY(s);
   }
@@ -1657,7 +1725,7 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
     const int blo = (j0 == 0) ? 0 : j0 + 1;
     for (int b = j1; b >= blo; --b) {
       const double dtk = (b == 0 || b == nsteps) ? 0.5 * dt : dt;
-      KickArgs ka = kick_args(c, dtk, b);
+      KickArgs ka = kick_args(c, dtk, tide_row(c, b * dt, b));
       j.pre = st_psi(seg, b);
       const float2* Hb = st_H(seg, b);
       // the adjoint kick follows the kick pass's implementation (staged or direct)
@@ -1778,6 +1846,11 @@ static wdm_status group_enqueue(wdm_group* g, int32_t nsteps, const double* dts,
   std::vector<double> dt(dts, dts + n);
   std::vector<long long> ver(n);
   for (size_t i = 0; i < n; ++i) {
+    const wdm_ctx* c = g->m[i];
+    if (c->tide_on == 1 && c->tide.size() > 6 && c->tide_dt > 0.0)
+      return group_fail(WDM_ERR_STATE, "wdm_group_step: member " + std::to_string(i) +
+                                           " has a clocked tidal schedule of several rows; a replayed graph "
+                                           "cannot follow the time (use wdm_step)");
     wdm_status s = prepare_capture(g->m[i], dt[i]);
     if (s != WDM_OK) return group_fail(s, "wdm_group_step: member " + std::to_string(i) + ": " + g->m[i]->err);
     ver[i] = g->m[i]->version;

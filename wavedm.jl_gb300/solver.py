@@ -190,16 +190,15 @@ def SPE3D_waveDM(*, Nx=64, Ny=None, Nz=None, Xmax=10.0, Ymax=None, Zmax=None, Nt
         done = 0
         total = Nt - 1
         psi_last_t = None
+        if tidal is not None:
+            # one clocked schedule for the run: row s is the tide at time s dt
+            ctx.set_tidal([tidal(t0) for t0 in np.arange(total + 1) * dt], t_first=0.0, t_step=dt)
         while done < total:
             n = min(stride, total - done)
-            if tidal is not None:
-                ctx.set_tidal([tidal(t0) for t0 in (done + np.arange(n + 1)) * dt])
             if outputdir is not None and done + n == total and n > 1:
                 # the state one step before the end (psi_last_t of the reference loop)
                 ctx.step(n - 1, dt, t0=done * dt, mode=mode)
                 psi_last_t = ctx.get_psi()
-                if tidal is not None:
-                    ctx.set_tidal([tidal(t0) for t0 in (done + n - 1 + np.arange(2)) * dt])
                 ctx.step(1, dt, t0=(done + n - 1) * dt, mode=mode)
             else:
                 if outputdir is not None and done + n == total:
