@@ -128,13 +128,19 @@ def test_step_in_pieces_equals_one_call(wdm, path):
             ctx.step(1, dt, t0=s * dt, mode=str(d["mode"]))
         psi = ctx.get_psi()
     assert spe.rel_l2(psi, d["psi"]) < 2e-5
-    # the same pieces bit for bit as one call over the clocked schedule
+    # One call over the clocked schedule: the same kicks at the same times.
+    # The reference loop and the Lie step repeat the same launches either way
+    # (bit for bit); a Strang call merges the half kicks between its steps,
+    # which pieces of one step each cannot, so those agree to rounding.
     with _ctx_for_golden(wdm, d) as ctx:
         if "tidal" in d:
             ctx.set_tidal(d["tidal"], t_first=0.0, t_step=dt)
         ctx.step(steps, dt, t0=0.0, mode=str(d["mode"]))
         one = ctx.get_psi()
-    assert np.array_equal(psi, one)
+    if str(d["mode"]) == "strang":
+        assert spe.rel_l2(psi, one) < 2e-6
+    else:
+        assert np.array_equal(psi, one)
 
 
 def test_kick_follows_the_tidal_clock(wdm):

@@ -92,18 +92,21 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
 }
 
 struct DriftOp {
-  // precise form: per-axis phases th_a = k_a^2 dt/2 mod 2 pi built in FP64 and
-  // kept as FP32 (hi, lo) pairs.  Per mode the three phases are summed in
-  // float-float, reduced to |r| <= pi, and the factor is applied as
-  // v + v (exp(-i r) - 1) from one sincos of r/2; the 1/(nx ny nz)
-  // normalisation is an FP32 hi + lo pair.  Every mode then rounds its own
-  // factor independently: a product of per-axis FP32 factors instead repeats
-  // the same table rounding over whole planes of modes, step after step, and
+  // precise form: the factor exp(-i (kx^2 + ky^2 + kz^2) dt/2) / (nx ny nz)
+  // separates into a factor per z line and one per mode along the line.
+  // cxy[my * nxy + mx] = exp(-i (kx^2 + ky^2) dt/2) / (nx ny nz) and
+  // cz[mz] = exp(-i kz^2 dt/2) are built in FP64 (phases reduced mod 2 pi in
+  // double) and kept as FP32 (hi, lo) pairs in the twiddle layout
+  // (pack_twiddle); a point takes two compensated complex products
+  // (twiddle_mul), so each factor acts with its FP64 modulus and phase and
+  // only the two roundings of the product remain, unbiased from point to
+  // point and step to step.  A plain FP32 table would instead repeat one
+  // fixed rounding of |factor| over whole planes of modes every step, which
   // shows up as a mass drift.
-  const float2* cx;
-  const float2* cy;
-  const float2* cz;
-  float scale_lo;
+  const float4* cxy;
+  const float4* cz;
+  int nxy;                // row length of cxy (nx)
+  int rot;                // cz holds entries flagged as rotated (sin = +-1/2)
   // plain form: k_a^2 tables and the FP32 phase k^2 dt/2
   const float* kx2;
   const float* ky2;
@@ -112,22 +115,14 @@ struct DriftOp {
   float scale;
   float sign;             // +1: exp(-i k^2 dt/2); -1: its conjugate (the drift adjoint)
   int precise;
-  long long tab_bstride;  // per-batch-item stride of the phase tables (0 = shared)
   static constexpr bool TABLE = false;
-  __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int b) const {
+  __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int) const {
     if (precise) {
-      const long long o = b * tab_bstride;
-      const float2 tx = cx[o + mx], ty = cy[o + my], tz = cz[o + pos];
-      const float s1 = tx.x + ty.x;
-      const float e1 = two_sum_err(tx.x, ty.x, s1);
-      const float s2 = s1 + tz.x;
-      const float e2 = two_sum_err(s1, tz.x, s2);
-      const float lo = ((e1 + e2) + (tx.y + ty.y)) + tz.y;
-      const float n = rintf(s2 * 0.15915494309189535f);
-      const float r = fmaf(-n, 6.28318548202514648f, s2) + fmaf(-n, -1.7484555e-07f, lo);
-      const float2 em1 = expm1_neg_i(sign * r);  // exp(-i r) - 1 (or its conjugate)
-      const float2 w = cadd(v, cmul(v, em1));
-      return make_float2(fmaf(w.x, scale, w.x * scale_lo), fmaf(w.y, scale, w.y * scale_lo));
+      const bool conj = sign < 0.f;
+      const float4 wz = cz[pos];
+      const float4 wxy = cxy[(long long)my * nxy + mx];
+      const float2 u = rot ? twiddle_mul<true>(v, wz, conj) : twiddle_mul<false>(v, wz, conj);
+      return twiddle_mul<false>(u, wxy, conj);
     }
     const float th = sign * (kx2[mx] + ky2[my] + kz2[pos]) * half_dt;
     const float2 sc = sincos_plain(th);

@@ -121,7 +121,8 @@ struct wdm_ctx {
   float2* H = nullptr;
   float4 *twx = nullptr, *twy = nullptr, *twz = nullptr;  // (hi, lo) twiddles
   float *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
-  float2 *cx = nullptr, *cy = nullptr, *cz = nullptr;  // precise drift tables (cached per dt)
+  float4 *cxy = nullptr, *cz = nullptr;  // precise drift factors per z line / per kz (cached per dt)
+  int drift_rot = 0;                      // cz holds rotated (flagged) entries
   double tab_dt = NAN;
   float *mx = nullptr, *my = nullptr, *mz = nullptr;     // absorbing mask tables (cached per dt)
   double mask_dt = NAN;
@@ -357,26 +358,39 @@ static wdm_status upload_k2(wdm_ctx* c, float** dst, int n, double L) {
   return WDM_OK;
 }
 
-// Drift phase tables exp(-i k_a^2 dt/2) - 1 built in FP64 (argument reduced mod
-// 2 pi in double before sin).
+// Drift factors of the precise form, in FP64 with the phases reduced mod 2 pi
+// in double: cxy[my][mx] = exp(-i (kx^2 + ky^2) dt/2) / (nx ny nz) and
+// cz[mz] = exp(-i kz^2 dt/2), each kept as an FP32 (hi, lo) pair
+// (pack_twiddle).
 static wdm_status ensure_drift_tables(wdm_ctx* c, double dt) {
   if (c->tab_dt == dt) return WDM_OK;
-  const int n[3] = {c->d.nx, c->d.ny, c->d.nz};
-  const double L[3] = {c->d.lx, c->d.ly, c->d.lz};
-  float2* dst[3] = {c->cx, c->cy, c->cz};
-  for (int a = 0; a < 3; ++a) {
-    std::vector<float2> h(n[a]);
-    for (int m = 0; m < n[a]; ++m) {
-      // th = k^2 dt/2 reduced to [0, 2 pi) in FP64, kept as FP32 hi + lo
-      const double k = kval(m, n[a], L[a]);
-      double th = std::fmod(0.5 * k * k * dt, 2.0 * M_PI);
-      if (th < 0) th += 2.0 * M_PI;
-      const float hi = (float)th;
-      h[m] = make_float2(hi, (float)(th - (double)hi));
+  const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
+  auto phase = [&](int m, int n, double L) {
+    const double k = kval(m, n, L);
+    return std::fmod(0.5 * k * k * dt, 2.0 * M_PI);
+  };
+  std::vector<double> thx(nx), thy(ny);
+  for (int m = 0; m < nx; ++m) thx[m] = phase(m, nx, c->d.lx);
+  for (int m = 0; m < ny; ++m) thy[m] = phase(m, ny, c->d.ly);
+  const double scale = 1.0 / ((double)nx * ny * nz);
+  std::vector<float4> hxy((size_t)nx * ny), hz(nz);
+  for (int my = 0; my < ny; ++my)
+    for (int mx = 0; mx < nx; ++mx) {
+      const double th = std::fmod(thx[mx] + thy[my], 2.0 * M_PI);
+      hxy[(size_t)my * nx + mx] = pack_twiddle(scale * std::cos(th), -scale * std::sin(th));
     }
-    WDM_CU(c, cudaMemcpyAsync(dst[a], h.data(), n[a] * sizeof(float2), cudaMemcpyHostToDevice, c->st));
-    WDM_CU(c, cudaStreamSynchronize(c->st));
+  int rot = 0;
+  for (int m = 0; m < nz; ++m) {
+    const double th = phase(m, nz, c->d.lz);
+    hz[m] = pack_twiddle(std::cos(th), -std::sin(th));
+    unsigned bits;
+    std::memcpy(&bits, &hz[m].w, sizeof(bits));
+    rot |= (int)(bits & 1u);
   }
+  WDM_CU(c, cudaMemcpyAsync(c->cxy, hxy.data(), hxy.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
+  WDM_CU(c, cudaMemcpyAsync(c->cz, hz.data(), hz.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
+  WDM_CU(c, cudaStreamSynchronize(c->st));
+  c->drift_rot = rot;
   c->tab_dt = dt;
   return WDM_OK;
 }
@@ -613,18 +627,16 @@ static wdm_status drift_yz(wdm_ctx* c, double dt, float sign = 1.f, float2* data
   op.sign = sign;
   const bool precise = c->d.phase_mode == WDM_PHASE_PRECISE;
   if (precise) WDM_TRY(ensure_drift_tables(c, dt));
-  op.cx = c->cx;
-  op.cy = c->cy;
+  op.cxy = c->cxy;
   op.cz = c->cz;
+  op.nxy = c->d.nx;
+  op.rot = c->drift_rot;
   op.kx2 = c->kx2;
   op.ky2 = c->ky2;
   op.kz2 = c->kz2;
   op.half_dt = (float)(0.5 * dt);
-  const double scale = 1.0 / ((double)c->d.nx * c->d.ny * c->d.nz);
-  op.scale = (float)scale;
-  op.scale_lo = (float)(scale - (double)op.scale);
+  op.scale = (float)(1.0 / ((double)c->d.nx * c->d.ny * c->d.nz));
   op.precise = precise;
-  op.tab_bstride = 0;
   cudaError_t e;
   if ((e = run_pass(c, P_PSI_Y_FWD,
                     [&] { return c->ky->lfft(psi, lines_y(c, c->d.nx, c->d.nx, c->ncell), c->twy, false, B, c->st); })) !=
@@ -710,7 +722,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->st_rec) cudaStreamSynchronize(c->st_rec);
   if (c->st_cic) cudaStreamSynchronize(c->st_cic);
-  void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cx,  c->cy,
+  void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cxy,
                   c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->rb_rows, c->parts, c->T6b, c->flag, c->scratch_f,
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
@@ -936,8 +948,7 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   if ((s = upload_k2(c, &c->kx2, d->nx, d->lx)) != WDM_OK) return bail(s);
   if ((s = upload_k2(c, &c->ky2, d->ny, d->ly)) != WDM_OK) return bail(s);
   if ((s = upload_k2(c, &c->kz2, d->nz, d->lz)) != WDM_OK) return bail(s);
-  if ((s = dalloc(c, &c->cx, d->nx)) != WDM_OK) return bail(s);
-  if ((s = dalloc(c, &c->cy, d->ny)) != WDM_OK) return bail(s);
+  if ((s = dalloc(c, &c->cxy, (size_t)d->nx * d->ny)) != WDM_OK) return bail(s);
   if ((s = dalloc(c, &c->cz, d->nz)) != WDM_OK) return bail(s);
   if ((s = dalloc(c, &c->mx, d->nx)) != WDM_OK) return bail(s);
   if ((s = dalloc(c, &c->my, d->ny)) != WDM_OK) return bail(s);

