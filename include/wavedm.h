@@ -113,6 +113,25 @@ wdm_status wdm_set_tidal(wdm_ctx* ctx, const double* schedule, int32_t nsched, i
  * WDM_ERR_STATE.  No counterpart in the reference, whose tide is a function
  * of t evaluated on the host every step. */
 wdm_status wdm_set_tidal_clock(wdm_ctx* ctx, double t_first, double t_step);
+/* Where the tide is anchored, replacing the treatment of the tidal potential
+ * at the density maximum in add_tidal_potential! (src/physics/tidal_fields.jl:114-146).
+ * x_c is the centre of the cell of the largest |psi|^2 (the first such cell in
+ * memory order, as findmax picks it; baryons not included) and <x> the
+ * |psi|^2-weighted mean position, both taken by the density pass before each
+ * kick.  For Phi(x) = 1/2 x^T T x about the box centre:
+ *   WDM_TIDE_BOX_CENTRE  Phi(x) (the default);
+ *   WDM_TIDE_REFERENCE   Phi(x) - Phi(x_c): the potential the reference's code
+ *                        leaves (tidal_fields.jl:114).  Its gradient
+ *                        cancellation (:115, :126-146) assigns to its local
+ *                        argument and discards the result, so the caller's
+ *                        potential keeps its gradient;
+ *   WDM_TIDE_DENSITY_MAX Phi(x) - Phi(x_c) - grad Phi(x_c).(x - <x>): the value and
+ *                        gradient removed at x_c as that cancellation computes
+ *                        them, = 1/2 (x-x_c)^T T (x-x_c) + (T x_c).(<x> - x_c).
+ * Modes 0 and 1 differ by a uniform potential (a global phase of psi).
+ * wdm_adjoint refuses modes 1 and 2 (WDM_ERR_UNSUPPORTED). */
+typedef enum { WDM_TIDE_BOX_CENTRE = 0, WDM_TIDE_REFERENCE = 1, WDM_TIDE_DENSITY_MAX = 2 } wdm_tide_centering;
+wdm_status wdm_set_tidal_centering(wdm_ctx* ctx, int32_t mode);
 /* baryon particles (positions [n][3] and masses [n], doubles), CIC-deposited
  * into the density before every Poisson solve; n == 0 removes them. */
 wdm_status wdm_set_particles(wdm_ctx* ctx, const double* pos, const double* mass, int64_t n);
@@ -140,6 +159,18 @@ wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32
 /* the same, returning once the graph is enqueued on the group's stream (check
  * the members with wdm_check_finite after synchronising the stream) */
 wdm_status wdm_group_step_async(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode);
+/* How the group runs a call, chosen on its first call by timing both on the
+ * members' own state (saved and put back):
+ *   0  the members' pass launches, captured into one CUDA graph;
+ *   1  one persistent cooperative kernel for all passes of all members and
+ *      steps, a device-wide barrier between passes (its waits bounded: an
+ *      abandoned one is reported as WDM_ERR_CUDA), replayed from a graph.
+ *      It covers members with axis lengths 16..128 without baryon particles
+ *      and with a tide that is constant during the call.
+ * sched: the choice (-1 before the first call); ms[0], ms[1]: the timed
+ * milliseconds of two steps under each (-1 when not timed).  The environment
+ * variable WDM_GROUP_SCHEDULE=graph|persistent forces the choice. */
+wdm_status wdm_group_schedule(const wdm_group* g, int32_t* sched, double* ms);
 /* the group's cudaStream_t */
 void* wdm_group_stream(const wdm_group* g);
 /* kernel launches executed by the group's graph replays so far */

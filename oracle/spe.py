@@ -20,8 +20,8 @@ Reference sources restated here (paths inside the WaveDM.jl project):
 * ``src/solver/KDK.jl:52-73,88-101``   kick exp(-i dt Phi) psi, fft, phase, ifft, mask
 * ``src/simulation_main.jl:536-547``   literal loop order K(dt/2) D(dt) per iteration
 * ``docs/src/algorithms.md:120-142``   symmetric Strang K(dt/2) D(dt) K(dt/2)
-* ``src/physics/tidal_fields.jl:114-146`` tidal potential with value and gradient
-  removed at the centre (the quadratic form 1/2 x^T T x has neither)
+* ``src/physics/tidal_fields.jl:114-146`` tidal potential with its value (and,
+  as an option, its gradient) removed at the density maximum
 * ``src/visualization/runtime.jl:210-238`` virial / kinetic / quantum / momentum sums
 * ``test/simulation_SPE3D_validation.jl:85-88`` relative L2 error definition
 
@@ -173,6 +173,65 @@ def tidal_potential(grid: Grid, T6):
     return 0.5 * (txx * X * X + tyy * Y * Y + tzz * Z * Z) + txy * X * Y + txz * X * Z + tyz * Y * Z
 
 
+def cancel_field_gradient_at_center(field, center, rho):
+    """Restatement of ``cancel_field_gradient_at_center!`` (``src/physics/tidal_fields.jl:126-146``),
+    returning the field it computes.
+
+    ``center`` is the (z, y, x) index of the density maximum.  The gradient is
+    the central difference at the centre in index units (``:127-129``); a
+    linear ramp (i - div(N, 2)) * gradient per axis, with the 1-based index i
+    (``:131-141``), is subtracted, and the density-weighted mean of the ramps
+    added back (``:143``).  Like Julia's indexing, a centre on the edge of the
+    grid has no central difference and raises.
+
+    The reference's function assigns ``field -= dp_field``, which rebinds its
+    local ``field`` to a new array, and its caller (``:115``) discards the
+    return value: the caller's potential keeps its gradient.  Callers of this
+    restatement choose whether to use the returned field.
+    """
+    nz, ny, nx = field.shape
+    cz, cy, cx = center
+    if not (0 < cx < nx - 1 and 0 < cy < ny - 1 and 0 < cz < nz - 1):
+        raise IndexError("density maximum on the edge of the grid: no central difference (BoundsError in Julia)")
+    dp_dx = (field[cz, cy, cx + 1] - field[cz, cy, cx - 1]) / 2
+    dp_dy = (field[cz, cy + 1, cx] - field[cz, cy - 1, cx]) / 2
+    dp_dz = (field[cz + 1, cy, cx] - field[cz - 1, cy, cx]) / 2
+    out = np.array(field, dtype=np.float64, copy=True)
+    ramp_x = (np.arange(1, nx + 1) - nx // 2)[None, None, :] * dp_dx * np.ones_like(out)
+    out = out - ramp_x
+    sum_pe = np.sum(ramp_x * rho)
+    ramp_y = (np.arange(1, ny + 1) - ny // 2)[None, :, None] * dp_dy * np.ones_like(out)
+    out = out - ramp_y
+    sum_pe += np.sum(ramp_y * rho)
+    ramp_z = (np.arange(1, nz + 1) - nz // 2)[:, None, None] * dp_dz * np.ones_like(out)
+    out = out - ramp_z
+    sum_pe += np.sum(ramp_z * rho)
+    return out + sum_pe / np.sum(rho)
+
+
+def centred_tidal_potential(grid: Grid, T6, rho, centering):
+    """The tidal potential after add_tidal_potential!'s treatment at the density
+    maximum (``src/physics/tidal_fields.jl:114-115``), for the quadratic tide.
+
+    ``rho`` is |psi|^2 of the state being kicked (the loop's ``rho``,
+    ``src/simulation_main.jl:550``); its maximum is the first in memory order,
+    as Julia's findmax takes it.
+    * ``"reference"``: the value at the maximum subtracted (``:114``), and the
+      gradient cancellation computed but not applied, as in the reference
+      (see cancel_field_gradient_at_center);
+    * ``"density_max"``: the field the gradient cancellation computes.
+    """
+    pot = tidal_potential(grid, T6) * np.ones(rho.shape)
+    c = np.unravel_index(int(np.argmax(rho)), rho.shape)
+    pot = pot - pot[c]
+    cancelled = cancel_field_gradient_at_center(pot, c, rho)
+    if centering == "reference":
+        return pot
+    if centering == "density_max":
+        return cancelled
+    raise ValueError(centering)
+
+
 def cic_deposit(grid: Grid, pos, mass):
     """Cloud-in-cell density (mass / dV per cell), periodic wrap.
 
@@ -234,6 +293,7 @@ class Physics:
     V_static: np.ndarray | None = None  # static external potential (z,y,x)
     rho_b: np.ndarray | None = None     # static baryon density added before the Poisson solve
     tidal: object = None                # callable t -> T6, or None
+    tidal_centering: str = "box_centre"  # "box_centre", "reference" or "density_max" (centred_tidal_potential)
 
     def tidal_at(self, t):
         if self.tidal is None:
@@ -251,7 +311,10 @@ def potential(psi, grid: Grid, phys: Physics, t):
         phi = phi + phys.V_static
     T6 = phys.tidal_at(t)
     if T6 is not None:
-        phi = phi + tidal_potential(grid, T6)
+        if phys.tidal_centering == "box_centre":
+            phi = phi + tidal_potential(grid, T6)
+        else:
+            phi = phi + centred_tidal_potential(grid, T6, np.abs(psi) ** 2, phys.tidal_centering)
     return phi
 
 

@@ -61,6 +61,12 @@ def test_autograd_function_matches_fp64_adjoint(wdm):
     assert float(loss) == pytest.approx(L_ref, rel=1e-5)
     assert spe.rel_l2(p.grad.cpu().numpy() / 2.0, g_ref) < 5e-4
     assert float(a.grad) / 2.0 == pytest.approx(da_ref, rel=1e-3)
+    # without a gradient to compute, the loss comes from the forward run alone
+    with torch.no_grad(), wdm.SPEContext(g.n, g.L, poisson_coeff=1.5) as ctx:
+        l0 = ctx.launch_count
+        loss_only = evolve_loss(p.detach(), a.detach(), ctx, nsteps, dt, rho, D, ckpt_every=3)
+        assert ctx.launch_count - l0 < 12 * nsteps  # a forward run: ~9 launches per step
+    assert float(loss_only) == pytest.approx(L_ref, rel=1e-5)
 
 
 def test_adjoint_workload5_shape_at_64(wdm):

@@ -89,3 +89,79 @@ def test_ensemble_of_three_sizes(wdm):
             ref = spe.run(inputs[k][b].astype(np.complex128), g, phys, dts[k], steps)
             assert spe.rel_l2(got[b], ref) < 2e-5
         members[k].close()
+
+
+def _members(wdm, specs, centering=None):
+    out = []
+    for k, (n, batch, L) in enumerate(specs):
+        nx, ny, nz = n if isinstance(n, tuple) else (n, n, n)
+        ctx = wdm.SPEContext((nx, ny, nz), (L, L * ny / nx, L * nz / nx), poisson_coeff=1.0, batch=batch)
+        rng = np.random.default_rng(100 + k)
+        g = spe.Grid((nx, ny, nz), ctx.L)
+        X, Y, Z = g.coords()
+        psis = []
+        for b in range(batch):
+            amp = np.exp(-((X - 0.3 * b - 0.2) ** 2 + (Y + 0.1 * b) ** 2 + (Z - 0.15) ** 2) / (1.0 + 0.2 * b))
+            psis.append((amp * np.exp(0.2j * rng.standard_normal((nz, ny, nx)))).astype(np.complex64))
+        psis = np.stack(psis)
+        T = np.array([[0.05 * (b + 1), -0.02, -0.03 * (b + 1), 0.01, 0.0, 0.005] for b in range(batch)])
+        ctx.set_psi(psis)
+        ctx.set_tidal(T, per_item=True)
+        if centering and k == 0:
+            ctx.set_tidal_centering(centering)
+        out.append((ctx, psis, T, (L / nx) ** 2 / 6))
+    return out
+
+
+ENS_SPECS = [(16, 3, 8.0), (24, 2, 8.0), ((48, 32, 16), 1, 8.0), (64, 2, 10.0)]
+
+
+@pytest.mark.parametrize("mode", ["strang", "reference_loop", "lie"])
+def test_persistent_ensemble_equals_its_pass_launches(wdm, monkeypatch, mode):
+    """One cooperative launch per call (all passes, members and steps) gives the
+    bits of the same passes launched one by one with the register-tile line
+    passes and the direct x passes, including a tide anchored at the density
+    maximum (its words zeroed and refilled inside the launch)."""
+    monkeypatch.setenv("WDM_GROUP_SCHEDULE", "persistent")
+    monkeypatch.setenv("WDM_SCHEDULE", "tile,tile,tile,tile,direct,direct,direct")
+    steps = 4
+    mem = _members(wdm, ENS_SPECS, centering="density_max")
+    with wdm.Ensemble([m[0] for m in mem]) as ens:
+        l0 = ens.launch_count
+        ens.step(steps, [m[3] for m in mem], mode=mode)
+        ens.step(steps, [m[3] for m in mem], mode=mode)  # a replay continues the run
+        assert ens.schedule[0] == "persistent"
+        assert ens.launch_count - l0 == 2
+    for k, (ctx, psis, T, dt) in enumerate(mem):
+        got = ctx.get_psi()
+        with wdm.SPEContext(ctx.n, ctx.L, poisson_coeff=1.0, batch=ctx.batch) as solo:
+            solo.set_psi(psis)
+            solo.set_tidal(T, per_item=True)
+            if k == 0:
+                solo.set_tidal_centering("density_max")
+            solo.step(steps, dt, mode=mode)
+            solo.step(steps, dt, mode=mode)
+            assert np.array_equal(got, solo.get_psi()), k
+        ctx.close()
+
+
+def test_ensemble_schedule_choice_keeps_the_state(wdm, monkeypatch):
+    """The first call times both schedules on the members' own state and puts
+    it back: the run then equals a run under the chosen schedule forced."""
+    steps = 3
+    mem = _members(wdm, ENS_SPECS[:3])
+    with wdm.Ensemble([m[0] for m in mem]) as ens:
+        ens.step(steps, [m[3] for m in mem])
+        sched, ms = ens.schedule
+    assert sched in ("graph", "persistent")
+    assert ms["graph"] > 0 and ms["persistent"] > 0
+    auto = [m[0].get_psi() for m in mem]
+    for m in mem:
+        m[0].close()
+    monkeypatch.setenv("WDM_GROUP_SCHEDULE", sched)
+    mem = _members(wdm, ENS_SPECS[:3])
+    with wdm.Ensemble([m[0] for m in mem]) as ens:
+        ens.step(steps, [m[3] for m in mem])
+    for a, m in zip(auto, mem):
+        assert np.array_equal(a, m[0].get_psi())
+        m[0].close()

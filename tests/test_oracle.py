@@ -229,3 +229,41 @@ def test_loop_diagnostics_of_a_gaussian():
     assert d["dt_phase"] == pytest.approx(2 * g.spacing[0] ** 2 / np.pi)
     assert d["dt_grav"] == pytest.approx(2 * np.pi / np.abs(phi).max())
     assert d["dt_self"] == pytest.approx(2 * np.pi / 0.5 / np.abs(psi).max())
+
+
+def _quadratic_tide_case(convention):
+    g = spe.Grid((20, 16, 12), (10.0, 8.0, 6.0), convention)
+    X, Y, Z = g.coords()
+    rng = np.random.default_rng(3)
+    # a positive density with a unique interior maximum off the box centre
+    rho = 0.1 + np.exp(-((X - 1.3) ** 2 + (Y + 0.7) ** 2 + (Z - 0.9) ** 2)) + 0.01 * rng.random((12, 16, 20))
+    T6 = (0.3, -0.1, -0.2, 0.05, -0.04, 0.02)
+    return g, rho, T6, (X, Y, Z)
+
+
+@pytest.mark.parametrize("convention", ["periodic", "reference"])
+def test_tide_about_density_max_closed_form(convention):
+    """The reference's value and gradient removal at the density maximum
+    (src/physics/tidal_fields.jl:114-146, restated step by step with its 1-based
+    ramps about div(N, 2)) equals, for the quadratic tide, the closed form
+    1/2 (x-x_c)^T T (x-x_c) + (T x_c).(<x> - x_c) the kernels evaluate."""
+    g, rho, T6, (X, Y, Z) = _quadratic_tide_case(convention)
+    c = np.unravel_index(int(np.argmax(rho)), rho.shape)
+    xc = np.array([X[0, 0, c[2]], Y[0, c[1], 0], Z[c[0], 0, 0]])
+    m = np.array([np.sum(rho * X), np.sum(rho * Y), np.sum(rho * Z)]) / np.sum(rho)
+    txx, tyy, tzz, txy, txz, tyz = T6
+    T = np.array([[txx, txy, txz], [txy, tyy, tyz], [txz, tyz, tzz]])
+    d = [X - xc[0], Y - xc[1], Z - xc[2]]
+    closed = 0.5 * sum(T[a, b] * d[a] * d[b] for a in range(3) for b in range(3)) + (T @ xc) @ (m - xc)
+    got = spe.centred_tidal_potential(g, T6, rho, "density_max")
+    assert np.allclose(got, closed, rtol=0, atol=1e-12 * np.abs(closed).max())
+    # what the reference's code leaves: only the value at x_c removed
+    ref = spe.centred_tidal_potential(g, T6, rho, "reference")
+    assert np.allclose(ref, spe.tidal_potential(g, T6) - 0.5 * xc @ T @ xc, rtol=0, atol=1e-13)
+
+
+def test_tide_gradient_cancellation_needs_an_interior_maximum():
+    g, rho, T6, _ = _quadratic_tide_case("periodic")
+    rho[0, 0, 0] = 10.0
+    with pytest.raises(IndexError):
+        spe.centred_tidal_potential(g, T6, rho, "density_max")

@@ -26,6 +26,7 @@ HOST, DEVICE = 0, 1
 STEP_MODES = {"strang": 0, "reference_loop": 1, "lie": 2}
 CONVENTIONS = {"periodic": 0, "reference": 1}
 PHASE_MODES = {"plain": 0, "precise": 1}
+TIDE_CENTERING = {"box_centre": 0, "reference": 1, "density_max": 2}
 
 
 class WdmDesc(C.Structure):
@@ -58,6 +59,7 @@ SIGNATURES = [
     ("wdm_set_static_potential", _i32, [_vp, _vp, _i32]),
     ("wdm_set_tidal", _i32, [_vp, _vp, _i32, _i32]),
     ("wdm_set_tidal_clock", _i32, [_vp, _d, _d]),
+    ("wdm_set_tidal_centering", _i32, [_vp, _i32]),
     ("wdm_set_particles", _i32, [_vp, _vp, _vp, _i64]),
     ("wdm_step", _i32, [_vp, _i32, _d, _d, _i32]),
     ("wdm_step_async", _i32, [_vp, _i32, _d, _d, _i32]),
@@ -88,6 +90,7 @@ SIGNATURES = [
     ("wdm_group_step", _i32, [_vp, _i32, _vp, _i32]),
     ("wdm_group_step_async", _i32, [_vp, _i32, _vp, _i32]),
     ("wdm_group_stream", _vp, [_vp]),
+    ("wdm_group_schedule", _i32, [_vp, C.POINTER(_i32), _vp]),
     ("wdm_group_launch_count", _i64, [_vp]),
 ]
 

@@ -19,6 +19,15 @@ class EvolveLoss(torch.autograd.Function):
         D = np.asarray(tidal_dir, np.float64)
         spe_ctx.set_psi(psi0.detach().contiguous())
         spe_ctx.set_tidal([float(amp) * D])
+        if not (ctx_.needs_input_grad[0] or ctx_.needs_input_grad[1]):
+            # no gradient wanted: the forward run alone (the adjoint costs ~2.5 of them)
+            spe_ctx.step(nsteps, dt)
+            rho = torch.empty(psi0.shape, dtype=torch.float32, device=psi0.device)
+            spe_ctx.get_rho(rho)
+            diff = rho.double() - torch.as_tensor(rho_target, device=psi0.device).double()
+            loss = (diff * diff).sum() * spe_ctx.cell_volume
+            spe_ctx.set_psi(psi0.detach().contiguous())  # psi is left at psi0, as wdm_adjoint leaves it
+            return loss.to(torch.float64)
         grad = torch.empty_like(psi0)
         loss, _, damp = spe_ctx.adjoint(nsteps, dt, rho_target, ckpt_every=ckpt_every, tidal_dir=D, grad_out=grad)
         ctx_.save_for_backward(grad)

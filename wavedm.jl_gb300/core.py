@@ -45,6 +45,7 @@ class SPEContext:
         lx, ly, lz = (float(v) for v in L)
         self.n = (nx, ny, nz)
         self.L = (lx, ly, lz)
+        self.convention = convention
         self.batch = int(batch)
         self.shape = (nz, ny, nx) if self.batch == 1 else (self.batch, nz, ny, nx)
         d = _abi.WdmDesc(nx, ny, nz, lx, ly, lz, _abi.CONVENTIONS[convention], float(poisson_coeff),
@@ -52,6 +53,12 @@ class SPEContext:
         h = C.c_void_p()
         check(self.lib.wdm_create(C.byref(d), C.byref(h)))
         self._h = h
+
+    @property
+    def cell_volume(self):
+        """dx dy dz of the grid convention (periodic: L/n, reference: L/(n - 1))."""
+        k = 0 if self.convention == "periodic" else 1
+        return float(np.prod([L / (n - k) for L, n in zip(self.L, self.n)]))
 
     # lifecycle -------------------------------------------------------------
     def close(self):
@@ -134,6 +141,12 @@ class SPEContext:
         self._check(self.lib.wdm_set_tidal(self.handle, C.c_void_p(s.ctypes.data), len(s), int(per_item)))
         if t_step is not None:
             self._check(self.lib.wdm_set_tidal_clock(self.handle, float(t_first or 0.0), float(t_step)))
+
+    def set_tidal_centering(self, mode):
+        """Anchor of the tide: "box_centre" (default), "reference" (its value at the
+        density maximum removed, as src/physics/tidal_fields.jl:114 leaves it) or
+        "density_max" (value and gradient removed there)."""
+        self._check(self.lib.wdm_set_tidal_centering(self.handle, _abi.TIDE_CENTERING[mode]))
 
     def set_particles(self, pos, mass):
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
@@ -312,6 +325,15 @@ class Ensemble:
     @property
     def launch_count(self):
         return int(self.lib.wdm_group_launch_count(self._h))
+
+    @property
+    def schedule(self):
+        """("graph" | "persistent" | None, {schedule: timed ms of two steps})."""
+        sched = C.c_int32(-1)
+        ms = (C.c_double * 2)()
+        check(self.lib.wdm_group_schedule(self._h, C.byref(sched), C.cast(ms, C.c_void_p)))
+        names = {0: "graph", 1: "persistent"}
+        return names.get(sched.value), {"graph": ms[0], "persistent": ms[1]}
 
     def close(self):
         if getattr(self, "_h", None):

@@ -268,28 +268,24 @@ struct NoOp {
   __device__ __forceinline__ float2 operator()(float2 v, int, int, int, int) const { return v; }
 };
 
-// One tile of LINES lines per CTA, loaded straight into registers (every
-// point of the tile in flight at once) and stored straight from them; the
-// hardware overlaps one resident CTA's loads with another's arithmetic.  This
-// is the default line pass (faster here than the persistent cp.async pipeline
-// above, which is kept behind WDM_LINE_PIPELINE for tuning).
+// One tile of LINES lines, loaded straight into registers (every point of the
+// tile in flight at once) and stored straight from them: lines line0 ..
+// line0 + LINES - 1 of batch item b, by threads tid = 0 .. threads_for<N>() - 1
+// (all of which, and any other threads of the CTA, reach the same barriers),
+// with the twiddle tables already in shared memory at tw and the exchange
+// buffer s (N * LPITCH entries).
 template <int N, int MODE, class Op>
-__global__ void __launch_bounds__(threads_for<N>(), min_blocks<N>())
-k_lfft_tile(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op) {
+__device__ __forceinline__ void lfft_tile_one(float2* __restrict__ data, const LineGeom& g, const float4* tw,
+                                              const Op& op, int line0, int b, float2* s, int tid) {
   using P = Plan<N>;
   constexpr int T = P::T;
   using Rad = typename P::Fwd;
   using Rev = typename Reverse<Rad>::type;
   constexpr int RS = RadInfo<Rad>::last;
-  constexpr int NTAB = MODE == 2 ? 2 : 1;
-  extern __shared__ float2 smem[];
-  float4* tw = reinterpret_cast<float4*>(smem);  // line fwd [| line rev] tables
-  float2* s = smem + 2 * NTAB * N;
-  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
-  const int l = threadIdx.x % LINES, t = threadIdx.x / LINES;
-  const int line = blockIdx.x * LINES + l;
+  const int l = tid % LINES, t = tid / LINES;
+  const int line = line0 + l;
   const bool ok = line < g.nlines;
-  float2* base = data + blockIdx.y * g.bstride + (ok ? line_base(g, line) : 0);
+  float2* base = data + b * g.bstride + (ok ? line_base(g, line) : 0);
   float2 v[N / T];
   lines_load<N>(v, base, g.pstride, ok, t);
   __syncthreads();
@@ -304,12 +300,28 @@ k_lfft_tile(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
 #pragma unroll
     for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), blockIdx.y);
+      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), b);
     run_stages<N, T, LPITCH, true>(Rev{}, v, s, tw + N, t, l);
     lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
   } else {
     lines_store<N, RS>(v, base, g.pstride, ok, t);
   }
+}
+
+// One tile of LINES lines per CTA (lfft_tile_one); the hardware overlaps one
+// resident CTA's loads with another's arithmetic.  This is the line pass where
+// the array has no tensor-map view (or the autotuner prefers it); the
+// persistent cp.async pipeline above is kept behind WDM_LINE_PIPELINE for
+// tuning.
+template <int N, int MODE, class Op>
+__global__ void __launch_bounds__(threads_for<N>(), min_blocks<N>())
+k_lfft_tile(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op) {
+  constexpr int NTAB = MODE == 2 ? 2 : 1;
+  extern __shared__ float2 smem[];
+  float4* tw = reinterpret_cast<float4*>(smem);  // line fwd [| line rev] tables
+  float2* s = smem + 2 * NTAB * N;
+  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
+  lfft_tile_one<N, MODE, Op>(data, g, tw, op, blockIdx.x * LINES, blockIdx.y, s, threadIdx.x);
 }
 
 template <int N, int MODE>
@@ -478,6 +490,9 @@ struct RhoArgs {
   // solve drops, so any value is exact; a value near the mean keeps the FP32
   // transform's rounding relative to rho - <rho> instead of rho.
   const float* shift;
+  // Non-null: accumulate the density maximum and moments of |psi|^2 into these
+  // zeroed words ([batch][CENTRE_WORDS]) for the tide frame of the next kick.
+  unsigned long long* centre = nullptr;
 };
 
 // ----------------------------------------------------------------------------
@@ -494,7 +509,22 @@ struct KickArgs {
   long long v_bstride;
   int precise;           // reduce the phase modulo 2 pi in float-float before sincos
   int* err = nullptr;    // error word of abandoned waits of the staged pass (may be null)
+  // Frame of the tide (used when tidal != 0): null keeps 1/2 x^T T x about the
+  // box centre.  Otherwise the words the last density pass left per batch
+  // item (CentreWords) give the density maximum x_c and the density's first
+  // moments; centre_mode 1 subtracts the tide's value at x_c, centre_mode 2
+  // its value and gradient there (see tide_frame).
+  const unsigned long long* centre = nullptr;
+  int centre_mode = 0;
 };
+
+// Per-batch-item words a density pass accumulates for the tide frame: [0] the
+// density maximum packed as (float bits of rho) << 32 | (0xffffffff - flat
+// cell index), so that the largest word is the largest rho at its first cell
+// in memory order; [1..4] the FP64 sums of rho, rho i, rho j, rho k over the
+// item (i, j, k the cell indices along x, y, z).  rho = |psi|^2, without the
+// baryon density.  Zeroed before every density pass that fills them.
+enum { CENTRE_WORDS = 5 };
 
 // psi * exp(-i dt pot).
 // Plain form: one FP32 sincos of pot*dt.

@@ -15,6 +15,7 @@
 
 #include "../../include/wavedm.h"
 #include "aux_kernels.cuh"
+#include "ensemble.cuh"
 #include "kernel_set.h"
 
 namespace wdm {
@@ -137,6 +138,10 @@ struct wdm_ctx {
   // clock of the schedule: row s is the tensor at time tide_t0 + s tide_dt
   // (tide_dt == 0: no clock, row s belongs to kick s of each wdm_step call)
   double tide_t0 = 0.0, tide_dt = 0.0;
+  // frame of the tide (wdm_tidal_centering) and the words the density passes
+  // leave for it ([batch][CENTRE_WORDS], allocated when a frame is chosen)
+  int tide_centre = 0;
+  unsigned long long* centre = nullptr;
   int* flag = nullptr;              // device words: [0] non-finite psi, [1] abandoned-wait bits
   float* scratch_f = nullptr;       // float field scratch [batch][ncell]
   float2* scratch_h = nullptr;      // half-spectrum scratch
@@ -508,6 +513,10 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.nonfinite = c->flag;
   ra.shift = c->shift;
   ra.err = c->flag + 1;
+  if (c->tide_centre && c->tide_on) {
+    WDM_CU(c, cudaMemsetAsync(c->centre, 0, sizeof(unsigned long long) * CENTRE_WORDS * B, c->st));
+    ra.centre = c->centre;
+  }
   cudaError_t e = run_pass(c, write_psi ? P_X_INV_RHO : P_DENSITY, [&] {
     return c->kx->x_inv_rho(c->psi, c->H, rows_psi(c, c->nparts > 0 ? LP_X_RHO_B : LP_X_RHO), c->hpitch, c->nhalf,
                             c->twx, ra, B, c->st);
@@ -574,6 +583,10 @@ static KickArgs kick_args(const wdm_ctx* c, double dt, int sched_row) {
   a.v_bstride = c->ncell;
   a.precise = c->d.phase_mode == WDM_PHASE_PRECISE;
   a.err = c->flag + 1;
+  if (c->tide_centre && a.tidal) {
+    a.centre = c->centre;
+    a.centre_mode = c->tide_centre;
+  }
   return a;
 }
 
@@ -727,7 +740,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
     if (p) cudaFree(p);
-  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc, c->diag_wsum, c->diag_wmin};
+  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc, c->diag_wsum, c->diag_wmin, c->centre};
   for (void* p : adj)
     if (p) cudaFree(p);
   for (auto* v : {&c->ck_psi, &c->ck_H, &c->slot_psi, &c->slot_H, &c->slot2_psi, &c->slot2_H})
@@ -1066,6 +1079,21 @@ wdm_status wdm_set_tidal_clock(wdm_ctx* c, double t_first, double t_step) {
   c->version++;
   c->tide_t0 = t_first;
   c->tide_dt = t_step;
+  return WDM_OK;
+}
+
+wdm_status wdm_set_tidal_centering(wdm_ctx* c, int32_t mode) {
+  if (!c) return fail(nullptr, WDM_ERR_INVALID, "null context");
+  if (mode != WDM_TIDE_BOX_CENTRE && mode != WDM_TIDE_REFERENCE && mode != WDM_TIDE_DENSITY_MAX)
+    return fail(c, WDM_ERR_INVALID, "wdm_set_tidal_centering: unknown mode");
+  if (mode != WDM_TIDE_BOX_CENTRE && !c->centre) {
+    WDM_TRY(dalloc(c, &c->centre, (size_t)CENTRE_WORDS * c->d.batch));
+    WDM_CU(c, cudaMemsetAsync(c->centre, 0, sizeof(unsigned long long) * CENTRE_WORDS * c->d.batch, c->st));
+    WDM_CU(c, cudaStreamSynchronize(c->st));
+  }
+  c->version++;
+  c->tide_centre = mode;
+  c->phi_valid = 0;  // the next kick needs a density pass that fills the words
   return WDM_OK;
 }
 
@@ -1625,6 +1653,9 @@ static wdm_status adjoint_impl(wdm_ctx* c, int nsteps, double dt, int ck, const 
   if (nsteps < 1 || ck < 1) return fail(c, WDM_ERR_INVALID, "wdm_adjoint: nsteps and ckpt_every must be >= 1");
   if (!rho_target || !grad || !loss) return fail(c, WDM_ERR_INVALID, "wdm_adjoint: null argument");
   WDM_TRY(check_tide_rows(c, 0.0, dt, nsteps + 1, "wdm_adjoint"));
+  if (c->tide_centre && c->tide_on)
+    return fail(c, WDM_ERR_UNSUPPORTED, "wdm_adjoint: the tide about the density maximum is not differentiated "
+                                        "(use WDM_TIDE_BOX_CENTRE)");
   const int B = c->d.batch;
   const size_t nc = (size_t)B * c->ncell, nh = (size_t)B * c->nhalf;
   if (!c->lam) WDM_TRY(dalloc(c, &c->lam, nc));
@@ -1791,7 +1822,7 @@ struct wdm_group {
   std::vector<wdm_ctx*> m;
   cudaStream_t st = nullptr;
   struct Entry {
-    int nsteps, mode;
+    int nsteps, mode, sched;
     std::vector<double> dts;
     std::vector<long long> versions;
     cudaGraphExec_t exec;
@@ -1799,7 +1830,21 @@ struct wdm_group {
   };
   std::vector<Entry> cache;
   int64_t launches = 0;
+  // schedule: GROUP_GRAPH (the members' pass launches in one captured graph)
+  // or GROUP_PERSISTENT (one cooperative launch of k_ensemble per call);
+  // chosen by timing both on the first call (see choose_schedule)
+  int sched = -1;
+  double sched_ms[2] = {-1.0, -1.0};
+  // the persistent kernel's member table on the device, for (dts, mode, versions)
+  EnsMember* dmem = nullptr;
+  unsigned* dwords = nullptr;
+  std::vector<double> dmem_dts;
+  std::vector<long long> dmem_versions;
+  int dmem_mode = -1;
+  size_t ens_smem = 0;
+  int ens_grid = 0;
 };
+enum { GROUP_GRAPH = 0, GROUP_PERSISTENT = 1 };
 
 // Everything a captured step sequence must not do inside the capture (table
 // uploads with a host sync, the first potential) is done here, eagerly.
@@ -1841,6 +1886,8 @@ wdm_status wdm_group_destroy(wdm_group* g) {
   if (!g) return WDM_OK;
   if (g->st) cudaStreamSynchronize(g->st);
   for (auto& en : g->cache) cudaGraphExecDestroy(en.exec);
+  if (g->dmem) cudaFree(g->dmem);
+  if (g->dwords) cudaFree(g->dwords);
   if (g->st) cudaStreamDestroy(g->st);
   delete g;
   return WDM_OK;
@@ -1848,10 +1895,265 @@ wdm_status wdm_group_destroy(wdm_group* g) {
 
 int64_t wdm_group_launch_count(const wdm_group* g) { return g ? g->launches : 0; }
 
-// Capture (first time) and launch the graph of nsteps steps on the group's
-// stream without waiting for it.
+// The persistent kernel covers members whose axis lengths it is built for,
+// without baryon particles and with a tide that is constant during the call.
+static bool persistent_ok(const wdm_group* g) {
+  for (const wdm_ctx* c : g->m) {
+    if (!ens_size_supported(c->d.nx) || !ens_size_supported(c->d.ny) || !ens_size_supported(c->d.nz)) return false;
+    if (c->nparts > 0) return false;
+    if (c->tide_on == 1 && c->tide.size() > 6) return false;
+  }
+  return true;
+}
+
+// Member table of the persistent kernel for these time steps and mode: the
+// arguments of the direct x passes and the register-tile line passes that the
+// pass launches of step_impl would get.
+static wdm_status build_members(wdm_group* g, const std::vector<double>& dt, int mode,
+                                const std::vector<long long>& ver) {
+  if (g->dmem && g->dmem_dts == dt && g->dmem_mode == mode && g->dmem_versions == ver) return WDM_OK;
+  const int n = (int)g->m.size();
+  std::vector<EnsMember> h((size_t)n);
+  std::vector<int> nx(n), ny(n), nz(n);
+  for (int i = 0; i < n; ++i) {
+    wdm_ctx* c = g->m[i];
+    EnsMember& e = h[i];
+    e.nx = nx[i] = c->d.nx;
+    e.ny = ny[i] = c->d.ny;
+    e.nz = nz[i] = c->d.nz;
+    e.batch = c->d.batch;
+    e.psi = c->psi;
+    e.H = c->H;
+    e.hpitch = c->hpitch;
+    e.nhalf = c->nhalf;
+    e.twx = c->twx;
+    e.twy = c->twy;
+    e.twz = c->twz;
+    e.rows = rows_psi(c);
+    e.rows.impl = X_IMPL_DIRECT;
+    e.ly_psi = lines_y(c, c->d.nx, c->d.nx, c->ncell);
+    e.lz_psi = lines_z(c, c->d.nx, c->d.nx, c->ncell);
+    e.ly_h = lines_y(c, c->nxh, c->hpitch, c->nhalf);
+    e.lz_h = lines_z(c, c->nxh, c->hpitch, c->nhalf);
+    e.kick_half = kick_args(c, 0.5 * dt[i], 0);
+    e.kick_full = kick_args(c, dt[i], 0);
+    RhoArgs ra{};
+    const bool mask = c->d.absorb_alpha != 0.0;
+    ra.mx = mask ? c->mx : nullptr;
+    ra.my = mask ? c->my : nullptr;
+    ra.mz = mask ? c->mz : nullptr;
+    ra.write_psi = 1;
+    ra.nonfinite = c->flag;
+    ra.shift = c->shift;
+    ra.err = c->flag + 1;
+    e.centre = (c->tide_centre && c->tide_on) ? c->centre : nullptr;
+    ra.centre = e.centre;
+    e.rho = ra;
+    DriftOp op{};
+    op.sign = 1.f;
+    op.cxy = c->cxy;
+    op.cz = c->cz;
+    op.nxy = c->d.nx;
+    op.rot = c->drift_rot;
+    op.kx2 = c->kx2;
+    op.ky2 = c->ky2;
+    op.kz2 = c->kz2;
+    op.half_dt = (float)(0.5 * dt[i]);
+    op.scale = (float)(1.0 / ((double)c->d.nx * c->d.ny * c->d.nz));
+    op.precise = c->d.phase_mode == WDM_PHASE_PRECISE;
+    e.drift = op;
+    PoissonOp po;
+    po.kx2 = c->kx2;
+    po.ky2 = c->ky2;
+    po.kz2 = c->kz2;
+    po.coef = (float)(-c->d.poisson_coeff / ((double)c->d.nx * c->d.ny * c->d.nz));
+    e.poisson = po;
+  }
+  if (!g->dwords && cudaMalloc((void**)&g->dwords, sizeof(unsigned) * ENS_SYNC_WORDS) != cudaSuccess)
+    return group_fail(WDM_ERR_ALLOC, "wdm_group_step: cudaMalloc of the barrier words failed");
+  if (!g->dmem && cudaMalloc((void**)&g->dmem, sizeof(EnsMember) * n) != cudaSuccess)
+    return group_fail(WDM_ERR_ALLOC, "wdm_group_step: cudaMalloc of the member table failed");
+  g->ens_smem = ens_smem_bytes(nx.data(), ny.data(), nz.data(), n);
+  g->ens_grid = ens_grid(g->ens_smem);
+  if (g->ens_grid <= 0) return group_fail(WDM_ERR_CUDA, "wdm_group_step: the persistent kernel does not fit");
+  for (int i = 0; i < n; ++i) h[i].rot = (int)(((long long)i * g->ens_grid) / n);
+  cudaError_t e = cudaMemcpyAsync(g->dmem, h.data(), sizeof(EnsMember) * n, cudaMemcpyHostToDevice, g->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->st);
+  if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("wdm_group_step: member table: ") + cudaGetErrorString(e));
+  g->dmem_dts = dt;
+  g->dmem_mode = mode;
+  g->dmem_versions = ver;
+  return WDM_OK;
+}
+
+// Enqueue one call on the group's stream under schedule `sched`: the captured
+// graph of the members' pass launches, or the graph of one persistent launch
+// (its barrier words cleared first).  Graphs are captured once per (nsteps,
+// mode, dts, member state, schedule) and replayed.
+static wdm_status group_launch(wdm_group* g, int32_t nsteps, const std::vector<double>& dt,
+                               const std::vector<long long>& ver, int32_t mode, int sched) {
+  const size_t n = g->m.size();
+  if (sched == GROUP_PERSISTENT) WDM_TRY(build_members(g, dt, mode, ver));
+  wdm_group::Entry* hit = nullptr;
+  for (auto& en : g->cache)
+    if (en.nsteps == nsteps && en.mode == mode && en.sched == sched && en.dts == dt && en.versions == ver) hit = &en;
+  if (!hit) {
+    if (g->cache.size() >= 8) {
+      cudaGraphExecDestroy(g->cache.front().exec);
+      g->cache.erase(g->cache.begin());
+    }
+    cudaError_t e = cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
+    int64_t launches = 0;
+    wdm_status bad = WDM_OK;
+    std::string why;
+    if (sched == GROUP_PERSISTENT) {
+      wdm_ctx* c0 = g->m[0];
+      const long long l0 = tl_kernel_launches;
+      e = cudaMemsetAsync(g->dwords, 0, sizeof(unsigned) * ENS_SYNC_WORDS, g->st);
+      if (e == cudaSuccess)
+        e = ens_launch(g->dmem, (int)n, nsteps, mode, g->dwords, c0->flag + 1, g->ens_smem, g->ens_grid, g->st);
+      launches = tl_kernel_launches - l0;
+      if (e != cudaSuccess) {
+        bad = WDM_ERR_CUDA;
+        why = std::string("persistent launch: ") + cudaGetErrorString(e);
+      }
+    } else {
+      for (size_t i = 0; i < n && bad == WDM_OK; ++i) {
+        wdm_ctx* c = g->m[i];
+        cudaStream_t own = c->st;
+        const bool prof = c->prof.on;
+        const int64_t l0 = c->launch_count;
+        c->st = g->st;
+        c->prof.on = false;
+        bad = step_impl(c, nsteps, dt[i], 0.0, mode);
+        if (bad != WDM_OK) why = c->err;
+        launches += c->launch_count - l0;
+        c->launch_count = l0;  // counted when the graph runs
+        c->st = own;
+        c->prof.on = prof;
+      }
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(g->st, &graph);
+    if (bad != WDM_OK || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      if (bad != WDM_OK) return group_fail(bad, "wdm_group_step: capture: " + why);
+      return group_fail(WDM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    g->cache.push_back({nsteps, mode, sched, dt, ver, exec, launches});
+    hit = &g->cache.back();
+  }
+  cudaError_t e = cudaGraphLaunch(hit->exec, g->st);
+  if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  g->launches += hit->launches;
+  for (size_t i = 0; i < n; ++i) g->m[i]->launch_count += hit->launches / (int64_t)n;
+  return WDM_OK;
+}
+
+// Time both schedules on the members' own state (saved first and put back
+// after each timing), two steps each after a warm-up call, and keep the
+// faster (the graph of pass launches within 3%).  WDM_GROUP_SCHEDULE=graph or
+// =persistent forces the choice.
+static wdm_status choose_schedule(wdm_group* g, const std::vector<double>& dt, const std::vector<long long>& ver,
+                                  int32_t mode) {
+  if (const char* env = std::getenv("WDM_GROUP_SCHEDULE")) {
+    if (!std::strcmp(env, "graph")) {
+      g->sched = GROUP_GRAPH;
+      return WDM_OK;
+    }
+    if (!std::strcmp(env, "persistent")) {
+      if (!persistent_ok(g)) return group_fail(WDM_ERR_UNSUPPORTED, "WDM_GROUP_SCHEDULE=persistent: a member's "
+                                                                   "size or options are not covered by the persistent kernel");
+      g->sched = GROUP_PERSISTENT;
+      return WDM_OK;
+    }
+  }
+  if (!persistent_ok(g)) {
+    g->sched = GROUP_GRAPH;
+    return WDM_OK;
+  }
+  const size_t n = g->m.size();
+  std::vector<float2*> keep(2 * n, nullptr);
+  auto release = [&]() {
+    for (float2* p : keep)
+      if (p) cudaFree(p);
+  };
+  for (size_t i = 0; i < n; ++i) {
+    wdm_ctx* c = g->m[i];
+    const size_t np = (size_t)c->ncell * c->d.batch, nh = (size_t)c->nhalf * c->d.batch;
+    if (cudaMalloc((void**)&keep[2 * i], sizeof(float2) * np) != cudaSuccess ||
+        cudaMalloc((void**)&keep[2 * i + 1], sizeof(float2) * nh) != cudaSuccess) {
+      release();
+      g->sched = GROUP_GRAPH;  // no room to time both: keep the launches
+      cudaGetLastError();
+      return WDM_OK;
+    }
+    cudaMemcpyAsync(keep[2 * i], c->psi, sizeof(float2) * np, cudaMemcpyDeviceToDevice, g->st);
+    cudaMemcpyAsync(keep[2 * i + 1], c->H, sizeof(float2) * nh, cudaMemcpyDeviceToDevice, g->st);
+  }
+  // the tide-frame words of the last density pass belong to the saved state too
+  std::vector<std::vector<unsigned long long>> words(n);
+  cudaStreamSynchronize(g->st);
+  for (size_t i = 0; i < n; ++i)
+    if (g->m[i]->centre) {
+      words[i].resize((size_t)CENTRE_WORDS * g->m[i]->d.batch);
+      cudaMemcpy(words[i].data(), g->m[i]->centre, sizeof(unsigned long long) * words[i].size(), cudaMemcpyDeviceToHost);
+    }
+  auto restore = [&]() {
+    for (size_t i = 0; i < n; ++i) {
+      wdm_ctx* c = g->m[i];
+      cudaMemcpyAsync(c->psi, keep[2 * i], sizeof(float2) * c->ncell * c->d.batch, cudaMemcpyDeviceToDevice, g->st);
+      cudaMemcpyAsync(c->H, keep[2 * i + 1], sizeof(float2) * c->nhalf * c->d.batch, cudaMemcpyDeviceToDevice, g->st);
+      if (!words[i].empty())
+        cudaMemcpyAsync(c->centre, words[i].data(), sizeof(unsigned long long) * words[i].size(),
+                        cudaMemcpyHostToDevice, g->st);
+    }
+    cudaStreamSynchronize(g->st);
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  wdm_status st = WDM_OK;
+  for (int sch = 0; sch < 2 && st == WDM_OK; ++sch) {
+    st = group_launch(g, 2, dt, ver, mode, sch);  // warm-up (and capture)
+    restore();
+    if (st != WDM_OK) break;
+    cudaEventRecord(e0, g->st);
+    st = group_launch(g, 2, dt, ver, mode, sch);
+    cudaEventRecord(e1, g->st);
+    restore();
+    if (st != WDM_OK) break;
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = group_fail(WDM_ERR_CUDA, "wdm_group_step: schedule timing failed");
+      break;
+    }
+    g->sched_ms[sch] = ms;
+  }
+  cudaStreamSynchronize(g->st);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  release();
+  if (st != WDM_OK) return st;
+  for (wdm_ctx* c : g->m) {  // the timing runs must leave no error bits behind
+    cudaMemsetAsync(c->flag, 0, 2 * sizeof(int), g->st);
+  }
+  cudaStreamSynchronize(g->st);
+  g->sched = g->sched_ms[GROUP_PERSISTENT] < 0.97 * g->sched_ms[GROUP_GRAPH] ? GROUP_PERSISTENT : GROUP_GRAPH;
+  return WDM_OK;
+}
+
+// Launch nsteps steps of every member on the group's stream without waiting.
 static wdm_status group_enqueue(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode) {
   if (!g || !dts || nsteps < 0) return group_fail(WDM_ERR_INVALID, "wdm_group_step: bad arguments");
+  if (mode != WDM_STEP_STRANG && mode != WDM_STEP_REFERENCE_LOOP && mode != WDM_STEP_LIE)
+    return group_fail(WDM_ERR_INVALID, "wdm_group_step: unknown step mode");
   if (nsteps == 0) return WDM_OK;
   const size_t n = g->m.size();
   std::vector<double> dt(dts, dts + n);
@@ -1866,51 +2168,17 @@ static wdm_status group_enqueue(wdm_group* g, int32_t nsteps, const double* dts,
     if (s != WDM_OK) return group_fail(s, "wdm_group_step: member " + std::to_string(i) + ": " + g->m[i]->err);
     ver[i] = g->m[i]->version;
   }
-  wdm_group::Entry* hit = nullptr;
-  for (auto& en : g->cache)
-    if (en.nsteps == nsteps && en.mode == mode && en.dts == dt && en.versions == ver) hit = &en;
-  if (!hit) {
-    if (g->cache.size() >= 8) {
-      cudaGraphExecDestroy(g->cache.front().exec);
-      g->cache.erase(g->cache.begin());
-    }
-    cudaError_t e = cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
-    int64_t launches = 0;
-    wdm_status bad = WDM_OK;
-    std::string why;
-    for (size_t i = 0; i < n && bad == WDM_OK; ++i) {
-      wdm_ctx* c = g->m[i];
-      cudaStream_t own = c->st;
-      const bool prof = c->prof.on;
-      const int64_t l0 = c->launch_count;
-      c->st = g->st;
-      c->prof.on = false;
-      bad = step_impl(c, nsteps, dt[i], 0.0, mode);
-      if (bad != WDM_OK) why = c->err;
-      launches += c->launch_count - l0;
-      c->launch_count = l0;  // counted when the graph runs
-      c->st = own;
-      c->prof.on = prof;
-    }
-    cudaGraph_t graph = nullptr;
-    e = cudaStreamEndCapture(g->st, &graph);
-    if (bad != WDM_OK || e != cudaSuccess) {
-      if (graph) cudaGraphDestroy(graph);
-      if (bad != WDM_OK) return group_fail(bad, "wdm_group_step: capture: " + why);
-      return group_fail(WDM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
-    }
-    cudaGraphExec_t exec = nullptr;
-    e = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    g->cache.push_back({nsteps, mode, dt, ver, exec, launches});
-    hit = &g->cache.back();
+  if (g->sched < 0 || (g->sched == GROUP_PERSISTENT && !persistent_ok(g))) WDM_TRY(choose_schedule(g, dt, ver, mode));
+  return group_launch(g, nsteps, dt, ver, mode, g->sched);
+}
+
+wdm_status wdm_group_schedule(const wdm_group* g, int32_t* sched, double* ms) {
+  if (!g || !sched) return group_fail(WDM_ERR_INVALID, "wdm_group_schedule: null argument");
+  *sched = g->sched;
+  if (ms) {
+    ms[0] = g->sched_ms[0];
+    ms[1] = g->sched_ms[1];
   }
-  cudaError_t e = cudaGraphLaunch(hit->exec, g->st);
-  if (e != cudaSuccess) return group_fail(WDM_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-  g->launches += hit->launches;
-  for (size_t i = 0; i < n; ++i) g->m[i]->launch_count += hit->launches / (int64_t)n;
   return WDM_OK;
 }
 

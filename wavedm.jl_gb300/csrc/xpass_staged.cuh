@@ -163,8 +163,8 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       phi[0][q] = v[q].x;
       phi[1][q] = v[q].y;
     }
-    float T6[6];
-    kick_tidal<N>(T6, a, b);
+    float T6[10];
+    kick_tidal<N>(T6, a, rg, b);
     auto release_b = [&]() {
       xrelease();
       if (un < nunits) {
@@ -255,6 +255,8 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     for (int r = 0; r < S::ROWS; ++r)
       if ((m >> r) & 1u) bulk_g2s(rbslot + r * S::RB_P, src + r * rg.pitch, (unsigned)(N * sizeof(float)), &xbar[0]);
   };
+  CentreSum cs;
+  cs.reset(-1);
   long long u = (long long)blockIdx.x * C::WARPS + warp;
   unsigned mcur = u < nunits ? rb_mask(u) : 0u;
   if (u < nunits) {
@@ -274,6 +276,8 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     float rho0[N / T];  // row A density at radix-RS slots
     float2 z[N / T];    // packed (rho_A, rho_B) at radix-RS slots
     float2 v[N / T];
+    CentreAcc ca;
+    ca.reset();
     if (!WDM_XSTAGE_WAIT(1)) WDM_XSTAGE_FAIL(a.err);
     auto release_p = [&]() {
       xrelease();
@@ -309,8 +313,8 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       release_p();
       if (with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
       float2* rowa = psi + b * rg.bstride + (long long)ra * rg.pitch;
-      rho_row_post<N>(v, a, rg, ra, true, rowa, rb_of(0), shift, 0, rho0, z, t);
-      rho_row_post<N>(vb, a, rg, ra + 1, true, rowa + rg.pitch, rb_of(1), shift, 1, rho0, z, t);
+      rho_row_post<N>(v, a, rg, ra, true, rowa, rb_of(0), shift, 0, rho0, z, t, ca);
+      rho_row_post<N>(vb, a, rg, ra + 1, true, rowa + rg.pitch, rb_of(1), shift, 1, rho0, z, t, ca);
       if (with_rb) release_r();
     } else {
 #pragma unroll
@@ -331,10 +335,11 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       if (half == 0 && with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
       const int r = ra + half;
       inv_rho_row<N>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb_of(half), shift, half,
-                     rho0, z, buf, tw, t);
+                     rho0, z, buf, tw, t, ca);
       if (half == 1 && with_rb) release_r();
     }
     }
+    if (a.centre) centre_pair_done<N>(a, rg, ca, cs, b, ra, true, t);
     if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t, (mcur >> (2 * g)) & 3u);
     mcur = mnext;
     reorder<N, T, RS, R1>(z, v);
@@ -342,6 +347,7 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     float2* hrow = H + b * hbstride + ra * hpitch;
     store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, true, t);
   }
+  if (a.centre && t == 0) cs.flush(a.centre);
 }
 
 // Adjoint kick (staged): the arithmetic of k_xw_adj_kick, with the H rows in
@@ -400,8 +406,8 @@ k_xs_adj_kick(float2* __restrict__ lam, const float2* __restrict__ H, float2* __
       phi[0][q] = v[q].x;
       phi[1][q] = v[q].y;
     }
-    float T6[6];
-    kick_tidal<N>(T6, a, b);
+    float T6[10];
+    kick_tidal<N>(T6, a, rg, b);
     float mu0[N / T];
     float2 z[N / T];
     float damp = 0.f;

@@ -191,7 +191,11 @@ struct XPlan<256> {
 template <>
 struct XPlan<384> {
   static constexpr int N = 384, T = 32;
+#if defined(WDM_X384_FWD_4446)
+  using Fwd = Radices<4, 4, 4, 6>;
+#else
   using Fwd = Radices<6, 4, 4, 4>;
+#endif
 };
 
 template <int N>
@@ -292,9 +296,10 @@ __device__ __forceinline__ void kick_points(float2* v, const float* phi, const f
   constexpr int R1 = RadInfo<typename XPlan<N>::Fwd>::first;
   const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
   const int y = r % rg.ny, z = r / rg.ny;
-  const float fy = a.y0 + a.dy * y, fz = a.z0 + a.dz * z;
-  // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2)
-  const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz;
+  // coordinates in the tide's frame (T6[6..8]: cell 0's, T6[9]: constant)
+  const float fy = T6[7] + a.dy * y, fz = T6[8] + a.dz * z;
+  // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2) + C
+  const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz + T6[9];
   const float lin = T6[3] * fy + T6[4] * fz;
 #pragma unroll
   for (int i = 0; i < N / (R1 * T); ++i)
@@ -304,7 +309,7 @@ __device__ __forceinline__ void kick_points(float2* v, const float* phi, const f
       const int x = slot_pos<N, T, R1>(t, i, k);
       float pot = phi[q];
       if (a.tidal) {
-        const float fx = a.x0 + a.dx * x;
+        const float fx = T6[6] + a.dx * x;
         pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
       }
       if (a.kerr != 0.f) pot += a.kerr * (v[q].x * v[q].x + v[q].y * v[q].y);
@@ -343,10 +348,133 @@ __device__ __forceinline__ void kick_row(float2* v, const float* phi, const floa
   }
 }
 
+// The tide's frame for batch item b from the words of the last density pass
+// (CentreWords).  x_c is the centre of the cell of the density maximum and
+// <x> the density-weighted mean position; for the quadratic tide
+// Phi(x) = 1/2 x^T T x:
+//   centre_mode 1: Phi(x) - Phi(x_c), the potential src/physics/tidal_fields.jl:114
+//     leaves (its gradient cancellation, :115 and :126-146, rebinds the
+//     function's local argument and does not change the caller's potential);
+//   centre_mode 2: Phi(x) - Phi(x_c) - grad Phi(x_c).(x - <x>), what that
+//     cancellation computes: = 1/2 (x - x_c)^T T (x - x_c) + (T x_c).(<x> - x_c).
+// Writes the frame's cell-0 coordinates to f[6..8] and the constant to f[9];
+// the arithmetic is FP64, once per unit of rows.
+static __device__ __noinline__ void tide_frame(float* f, const KickArgs& a, int nx, int ny, int b) {
+  const unsigned long long* w = a.centre + (long long)CENTRE_WORDS * b;
+  const unsigned flat = 0xffffffffu - (unsigned)(w[0] & 0xffffffffull);
+  const unsigned ix = flat % (unsigned)nx, iy = (flat / (unsigned)nx) % (unsigned)ny;
+  const unsigned iz = flat / ((unsigned)nx * (unsigned)ny);
+  const double xc = a.x0 + (double)a.dx * ix, yc = a.y0 + (double)a.dy * iy, zc = a.z0 + (double)a.dz * iz;
+  const double txx = f[0], tyy = f[1], tzz = f[2], txy = f[3], txz = f[4], tyz = f[5];
+  const double gx = txx * xc + txy * yc + txz * zc;
+  const double gy = txy * xc + tyy * yc + tyz * zc;
+  const double gz = txz * xc + tyz * yc + tzz * zc;
+  if (a.centre_mode == 1) {
+    f[9] = (float)(-0.5 * (xc * gx + yc * gy + zc * gz));
+    return;
+  }
+  const double s0 = __longlong_as_double((long long)w[1]);
+  const double inv = s0 > 0.0 ? 1.0 / s0 : 0.0;
+  const double mx = a.x0 + (double)a.dx * (__longlong_as_double((long long)w[2]) * inv);
+  const double my = a.y0 + (double)a.dy * (__longlong_as_double((long long)w[3]) * inv);
+  const double mz = a.z0 + (double)a.dz * (__longlong_as_double((long long)w[4]) * inv);
+  f[6] = (float)(-(double)a.dx * ix);
+  f[7] = (float)(-(double)a.dy * iy);
+  f[8] = (float)(-(double)a.dz * iz);
+  f[9] = (float)(gx * (mx - xc) + gy * (my - yc) + gz * (mz - zc));
+}
+
+// Tidal tensor of batch item b in T6[0..5] and the tide's frame in T6[6..9]
+// (cell-0 coordinates and a constant; the box centre and 0 without a frame).
 template <int N>
-__device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, int b) {
+__device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, const RowGeom& rg, int b) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
+  T6[6] = a.x0;
+  T6[7] = a.y0;
+  T6[8] = a.z0;
+  T6[9] = 0.f;
+  if (a.centre && a.tidal) tide_frame(T6, a, N, rg.ny, b);
+}
+
+// Density maximum and first moments of one row pair, per lane (CentreWords).
+struct CentreAcc {
+  float best;      // largest rho seen (-1: none)
+  unsigned cell;   // its flat cell index in the item
+  float s0[2];     // sum of rho of rows A and B
+  float si;        // sum of rho i (i the x index) over both rows
+  __device__ __forceinline__ void reset() {
+    best = -1.f;
+    cell = 0xffffffffu;
+    s0[0] = s0[1] = si = 0.f;
+  }
+  __device__ __forceinline__ void add(float d, unsigned c, int i, int half) {
+    if (d > best || (d == best && c < cell)) {
+      best = d;
+      cell = c;
+    }
+    s0[half] += d;
+    si = fmaf(d, (float)i, si);
+  }
+};
+
+// Per lane group: the pair sums carried in FP64 over the units a group runs,
+// written to the item's words when the item changes and at the end.
+struct CentreSum {
+  double s0, si, sj, sk;
+  unsigned long long key;
+  int item;
+  __device__ __forceinline__ void reset(int b) {
+    s0 = si = sj = sk = 0.0;
+    key = 0ull;
+    item = b;
+  }
+  __device__ __forceinline__ void flush(unsigned long long* words) const {
+    if (item < 0) return;
+    unsigned long long* w = words + (long long)CENTRE_WORDS * item;
+    atomicMax(w, key);
+    atomicAdd(reinterpret_cast<double*>(w + 1), s0);
+    atomicAdd(reinterpret_cast<double*>(w + 2), si);
+    atomicAdd(reinterpret_cast<double*>(w + 3), sj);
+    atomicAdd(reinterpret_cast<double*>(w + 4), sk);
+  }
+};
+
+// The row pair (ra, ra + 1) of item b is done: reduce its lanes' CentreAcc over
+// the lane group (T lanes) and add it to the group's CentreSum (on lane t = 0).
+template <int N>
+__device__ __forceinline__ void centre_pair_done(const RhoArgs& a, const RowGeom& rg, const CentreAcc& ca,
+                                                 CentreSum& cs, int b, int ra, bool ok, int t) {
+  constexpr int T = XCfg<N>::T;
+  float best = ca.best, s0a = ca.s0[0], s0b = ca.s0[1], si = ca.si;
+  unsigned cell = ca.cell;
+#pragma unroll
+  for (int off = T / 2; off > 0; off >>= 1) {
+    const float ob = __shfl_xor_sync(0xffffffffu, best, off, T);
+    const unsigned oc = __shfl_xor_sync(0xffffffffu, cell, off, T);
+    if (ob > best || (ob == best && oc < cell)) {
+      best = ob;
+      cell = oc;
+    }
+    s0a += __shfl_xor_sync(0xffffffffu, s0a, off, T);
+    s0b += __shfl_xor_sync(0xffffffffu, s0b, off, T);
+    si += __shfl_xor_sync(0xffffffffu, si, off, T);
+  }
+  if (t != 0 || !ok) return;
+  if (cs.item != b) {
+    cs.flush(a.centre);
+    cs.reset(b);
+  }
+  const int ja = ra % rg.ny, ka = ra / rg.ny, jb = (ra + 1) % rg.ny, kb = (ra + 1) / rg.ny;
+  cs.s0 += (double)s0a + (double)s0b;
+  cs.si += (double)si;
+  cs.sj += (double)s0a * ja + (double)s0b * jb;
+  cs.sk += (double)s0a * ka + (double)s0b * kb;
+  if (best >= 0.f) {
+    const unsigned long long key =
+        ((unsigned long long)__float_as_uint(best) << 32) | (unsigned long long)(0xffffffffu - cell);
+    if (key > cs.key) cs.key = key;
+  }
 }
 
 // After both rows of a pair used their baryon density: zero the flagged rows
@@ -378,14 +506,30 @@ __device__ __forceinline__ void clear_rb_pair(const RhoArgs& a, const RowGeom& r
   }
 }
 
+// The slice of an x pass one warp runs: warp units u0, u0 + ustride, ...,
+// with the twiddle tables of the pass (x fwd | x rev) in shared memory at tw
+// and this lane group's exchange buffer (XCfg<N>::NP entries) at buf.
+struct XSlice {
+  long long u0, ustride;
+  const float4* tw;
+  float2* buf;
+};
+
 template <int N, bool FWD>
-__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
-k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGeom rg, long long hpitch,
-          long long hbstride, const float4* __restrict__ twg, KickArgs a, XWork w) {
-  // psi_in == psi runs in place; a separate psi_in keeps the input state
-  WDM_XPASS_PROLOGUE
+__device__ __forceinline__ void xw_kick_units(const float2* psi_in, float2* psi, const float2* __restrict__ H,
+                                              const RowGeom& rg, long long hpitch, long long hbstride,
+                                              const KickArgs& a, const XWork& w, const XSlice& sl) {
+  using C = XCfg<N>;
+  constexpr int T = C::T;
+  using Rad = typename XPlan<N>::Fwd;
   using Rev = typename Reverse<Rad>::type;
-  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+  constexpr int R1 = RadInfo<Rad>::first;
+  const int lane = threadIdx.x & 31, g = lane / T, t = lane % T;
+  const float4* tw = sl.tw;
+  const float4* twr = tw + N;
+  float2* buf = sl.buf;
+  const long long nunits = w.units(C::GROUPS);
+  for (long long u = sl.u0; u < nunits; u += sl.ustride) {
     const long long pp = u * C::GROUPS + g;
     const bool ok = pp < (long long)w.pairs_per_item * w.batch;
     const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
@@ -400,8 +544,8 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       phi[0][q] = v[q].x;
       phi[1][q] = v[q].y;
     }
-    float T6[6];
-    kick_tidal<N>(T6, a, b);
+    float T6[10];
+    kick_tidal<N>(T6, a, rg, b);
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const int r = ra + half;
@@ -415,6 +559,17 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
   }
 }
 
+template <int N, bool FWD>
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
+k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGeom rg, long long hpitch,
+          long long hbstride, const float4* __restrict__ twg, KickArgs a, XWork w) {
+  // psi_in == psi runs in place; a separate psi_in keeps the input state
+  WDM_XPASS_PROLOGUE
+  (void)nunits;
+  xw_kick_units<N, FWD>(psi_in, psi, H, rg, hpitch, hbstride, a, w,
+                        XSlice{(long long)blockIdx.x * C::WARPS + warp, wstride, tw, buf});
+}
+
 // ----------------------------------------------------------------------------
 // P5: psi x-inverse (+mask) of rows A and B, rho = |psi|^2 (+rho_b) - shift,
 // packed R2C of (rho_A, rho_B) -> H rows A and B
@@ -426,7 +581,7 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
 template <int N>
 __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
                                              float2* row, const float* rb, float shift, int half, float* rho0,
-                                             float2* z, int t) {
+                                             float2* z, int t, CentreAcc& ca) {
   constexpr int T = XCfg<N>::T;
   constexpr int RS = RadInfo<typename XPlan<N>::Fwd>::last;
   if (a.write_psi) {
@@ -447,6 +602,10 @@ __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const 
       const float2 q = v[i * RS + k];
       float d = q.x * q.x + q.y * q.y;
       if (ok && a.nonfinite && !isfinite(d)) *a.nonfinite = 1;
+      if (a.centre) {
+        const int x = slot_pos<N, T, RS>(t, i, k);
+        ca.add(d, (unsigned)r * (unsigned)N + (unsigned)x, x, half);
+      }
       if (rb && ok) d += rb[slot_pos<N, T, RS>(t, i, k)];
       if (half == 0) rho0[i * RS + k] = d - shift;
       else z[i * RS + k] = make_float2(rho0[i * RS + k], d - shift);
@@ -459,18 +618,27 @@ __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const 
 template <int N>
 __device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
                                             float2* row, const float* rb, float shift, int half, float* rho0,
-                                            float2* z, float2* buf, const float4* tw, int t) {
+                                            float2* z, float2* buf, const float4* tw, int t, CentreAcc& ca) {
   using C = XCfg<N>;
   if (a.write_psi) run_wstages<N, C::T, C::NP, true>(typename XPlan<N>::Fwd{}, v, buf, tw, t);
-  rho_row_post<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, t);
+  rho_row_post<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, t, ca);
 }
 
 template <int N>
-__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
-k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
-             const float4* __restrict__ twg, RhoArgs a, XWork w) {
-  WDM_XPASS_PROLOGUE
-  for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
+__device__ __forceinline__ void xw_inv_rho_units(float2* __restrict__ psi, float2* __restrict__ H, const RowGeom& rg,
+                                                 long long hpitch, long long hbstride, const RhoArgs& a,
+                                                 const XWork& w, const XSlice& sl) {
+  using C = XCfg<N>;
+  constexpr int T = C::T;
+  using Rad = typename XPlan<N>::Fwd;
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
+  const int lane = threadIdx.x & 31, g = lane / T, t = lane % T;
+  const float4* tw = sl.tw;
+  float2* buf = sl.buf;
+  const long long nunits = w.units(C::GROUPS);
+  CentreSum cs;
+  cs.reset(-1);
+  for (long long u = sl.u0; u < nunits; u += sl.ustride) {
     const long long pp = u * C::GROUPS + g;
     const bool ok = pp < (long long)w.pairs_per_item * w.batch;
     const int b = ok ? (int)(pp / w.pairs_per_item) : 0;
@@ -479,6 +647,8 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     float rho0[N / T];  // row A density at radix-RS slots
     float2 z[N / T];    // packed (rho_A, rho_B) at radix-RS slots
     float2 v[N / T];
+    CentreAcc ca;
+    ca.reset();
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const int r = ra + half;
@@ -496,8 +666,9 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       }
       const bool rb_row = a.rho_b && (!a.rb_rows || a.rb_rows[r]);  // rows without baryon mass are zero
       const float* rb = rb_row ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
-      inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t);
+      inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t, ca);
     }
+    if (a.centre) centre_pair_done<N>(a, rg, ca, cs, b, ra, ok, t);
     if (a.rb_zero) {
       const unsigned fl = ok ? (!a.rb_rows ? 3u : (a.rb_rows[ra] ? 1u : 0u) | (a.rb_rows[ra + 1] ? 2u : 0u)) : 0u;
       clear_rb_pair<N>(a, rg, b, ra, ok, t, fl);
@@ -507,6 +678,17 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     float2* hrow = H + b * hbstride + ra * hpitch;
     store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, ok, t);
   }
+  if (a.centre && t == 0) cs.flush(a.centre);
+}
+
+template <int N>
+__global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
+k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
+             const float4* __restrict__ twg, RhoArgs a, XWork w) {
+  WDM_XPASS_PROLOGUE
+  (void)nunits;
+  xw_inv_rho_units<N>(psi, H, rg, hpitch, hbstride, a, w,
+                      XSlice{(long long)blockIdx.x * C::WARPS + warp, wstride, tw, buf});
 }
 
 // Plain C2C x pass (rows processed pairwise, scaled output).
