@@ -74,7 +74,7 @@ __device__ bool ens_grid_sync(unsigned* words, unsigned epoch, int* err) {
 // ---------------------------------------------------------------------------
 template <int N>
 constexpr size_t x_smem() {
-  return sizeof(float2) * (4 * (size_t)N + (size_t)ENS_WARPS * XCfg<N>::GROUPS * XCfg<N>::NP);
+  return sizeof(float2) * (2 * (size_t)N + (size_t)ENS_WARPS * XCfg<N>::GROUPS * XCfg<N>::NP);
 }
 
 template <int N, int NTAB>
@@ -86,10 +86,10 @@ template <int N, bool FWD>
 __device__ __noinline__ void x_kick(const EnsMember& m, const KickArgs& a, unsigned char* sm, int vb, int vg) {
   using C = XCfg<N>;
   float4* tw = reinterpret_cast<float4*>(sm);
-  load_twiddles(tw, m.twx + TW_X_FWD * N, 2 * N);
+  load_twiddles(tw, m.twx + TW_X_FWD * N, N);
   __syncthreads();
   const int warp = threadIdx.x >> 5, g = (threadIdx.x & 31) / C::T;
-  float2* buf = reinterpret_cast<float2*>(sm) + 4 * N + (size_t)(warp * C::GROUPS + g) * C::NP;
+  float2* buf = reinterpret_cast<float2*>(sm) + 2 * N + (size_t)(warp * C::GROUPS + g) * C::NP;
   const XWork w{m.rows.nrows / 2, m.batch};
   const XSlice sl{(long long)vb * ENS_WARPS + warp, (long long)vg * ENS_WARPS, tw, buf};
   xw_kick_units<N, FWD>(m.psi, m.psi, m.H, m.rows, m.hpitch, m.nhalf, a, w, sl);
@@ -100,13 +100,14 @@ template <int N>
 __device__ __noinline__ void x_rho(const EnsMember& m, unsigned char* sm, int vb, int vg) {
   using C = XCfg<N>;
   float4* tw = reinterpret_cast<float4*>(sm);
-  load_twiddles(tw, m.twx + TW_X_FWD * N, 2 * N);
+  load_twiddles(tw, m.twx + TW_X_FWD * N, N);
   __syncthreads();
   const int warp = threadIdx.x >> 5, g = (threadIdx.x & 31) / C::T;
-  float2* buf = reinterpret_cast<float2*>(sm) + 4 * N + (size_t)(warp * C::GROUPS + g) * C::NP;
+  float2* buf = reinterpret_cast<float2*>(sm) + 2 * N + (size_t)(warp * C::GROUPS + g) * C::NP;
   const XWork w{m.rows.nrows / 2, m.batch};
-  xw_inv_rho_units<N>(m.psi, m.H, m.rows, m.hpitch, m.nhalf, m.rho, w,
-                      XSlice{(long long)vb * ENS_WARPS + warp, (long long)vg * ENS_WARPS, tw, buf});
+  const XSlice sl{(long long)vb * ENS_WARPS + warp, (long long)vg * ENS_WARPS, tw, buf};
+  if (m.rho.centre) xw_inv_rho_units<N, true>(m.psi, m.H, m.rows, m.hpitch, m.nhalf, m.rho, w, sl);
+  else xw_inv_rho_units<N, false>(m.psi, m.H, m.rows, m.hpitch, m.nhalf, m.rho, w, sl);
   __syncthreads();
 }
 
@@ -169,6 +170,16 @@ __device__ void pass_lines(int n, float2* data, const LineGeom& g, const float4*
   }
 }
 
+// The tide's frame of item b of a member for its next kick (the frame words
+// of the last density pass; the kicks' tensor is constant during a call).
+__device__ void member_frame(const EnsMember& m, int b) {
+  const KickArgs& a = m.kick_full;
+  float T6[6];
+  for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[6 * b + q] : a.T6[q];
+  const double x0[3] = {a.x0, a.y0, a.z0}, d[3] = {a.dx, a.dy, a.dz};
+  tide_frame_of(m.frame + 4 * b, T6, m.centre + (long long)CENTRE_WORDS * b, m.centre_mode, m.nx, m.ny, x0, d);
+}
+
 // Pass p (0..7: P1..P8 of the step; 8: the closing half kick) of one member.
 __device__ void member_pass(const EnsMember& m, int p, int s, int mode, unsigned char* sm, int vb, int vg) {
   switch (p) {
@@ -195,12 +206,17 @@ k_ensemble(const EnsMember* __restrict__ mem, int nmem, int nsteps, int mode, un
   unsigned epoch = 0;
   for (int s = 0; s < nsteps; ++s) {
     for (int p = 0; p < 8; ++p) {
-      // the tide-frame words the density pass (p = 4) fills start at zero; the
-      // kicks that read them ran in phase 0, before the last barrier
+      // the tide-frame words the density pass (p = 4) fills start at zero (the
+      // frames of phase 0's kicks came from them before the last barrier), and
+      // the frames of the next kicks come from the filled words in phase 7
       if (p == 3 && blockIdx.x == 0)
         for (int m = 0; m < nmem; ++m)
           if (mem[m].centre)
             for (int i = threadIdx.x; i < CENTRE_WORDS * mem[m].batch; i += blockDim.x) mem[m].centre[i] = 0ull;
+      if (p == 7 && blockIdx.x == 0)
+        for (int m = 0; m < nmem; ++m)
+          if (mem[m].centre)
+            for (int b = threadIdx.x; b < mem[m].batch; b += blockDim.x) member_frame(mem[m], b);
       for (int m = 0; m < nmem; ++m) member_pass(mem[m], p, s, mode, esm, (blockIdx.x + mem[m].rot) % vg, vg);
       if (!ens_grid_sync(words, ++epoch, err)) return;
     }
@@ -219,7 +235,24 @@ size_t smem_for_axis(int n, int kind) {  // kind 0: x pass, 1: y lines, 2: z lin
   return 0;
 }
 
+__global__ void k_tide_frame(const unsigned long long* __restrict__ words, KickArgs a, int mode, int nx, int ny,
+                             int batch, float* __restrict__ frame) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < batch; b += gridDim.x * blockDim.x) {
+    float T6[6];
+    for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[6 * b + q] : a.T6[q];
+    const double x0[3] = {a.x0, a.y0, a.z0}, d[3] = {a.dx, a.dy, a.dz};
+    tide_frame_of(frame + 4 * b, T6, words + (long long)CENTRE_WORDS * b, mode, nx, ny, x0, d);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_tide_frame(const unsigned long long* words, const KickArgs& a, int mode, int nx, int ny, int batch,
+                              float* frame, cudaStream_t st) {
+  k_tide_frame<<<(batch + 127) / 128, 128, 0, st>>>(words, a, mode, nx, ny, batch, frame);
+  ++tl_kernel_launches;
+  return cudaGetLastError();
+}
 
 bool ens_size_supported(int n) {
   switch (n) {

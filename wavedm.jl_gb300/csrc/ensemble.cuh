@@ -27,6 +27,8 @@ struct EnsMember {
   DriftOp drift;
   PoissonOp poisson;
   unsigned long long* centre;     // tide-frame words to zero before each density pass (or null)
+  float* frame;                   // the tide's frame per item, made from them for the next kick
+  int centre_mode;                // 1 or 2 (wdm_tide_centering)
   int rot;                        // first virtual block of this member (spreads the members' tails)
 };
 
@@ -36,6 +38,11 @@ enum { ENS_SYNC_WORDS = 2 };
 // Error bit of an abandoned barrier wait (in the first member's error word).
 enum { WDM_DEVERR_BARRIER = 4 };
 constexpr int ENS_THREADS = 256;
+
+// The tide's frame (tide_frame_of) of every batch item for the next kick with
+// arguments a: one small launch after the density pass that filled `words`.
+cudaError_t launch_tide_frame(const unsigned long long* words, const KickArgs& a, int mode, int nx, int ny, int batch,
+                              float* frame, cudaStream_t st);
 
 // Axis lengths the persistent kernel is built for.
 bool ens_size_supported(int n);

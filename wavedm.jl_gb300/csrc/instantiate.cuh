@@ -198,12 +198,13 @@ struct Launch {
     const long long cap = (long long)resident_ctas<K>(XNT, smem) * sm_count();
     return dim3((unsigned)(ctas < cap ? ctas : cap));
   }
-  static cudaError_t x_inv_rho(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
-                               const float4* tw, const RhoArgs& a, int batch, cudaStream_t st) {
+  template <bool CEN>
+  static cudaError_t x_inv_rho_t(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
+                                 const float4* tw, const RhoArgs& a, int batch, cudaStream_t st) {
     cudaError_t e;
     XWork w;
     if (x_staged_ok(rg, hpitch, psi, H, a.rho_b) && (!a.rho_b || (a.rb_bstride * 4) % 16 == 0)) {
-      constexpr auto K = k_xs_inv_rho<N>;
+      constexpr auto K = k_xs_inv_rho<N, CEN>;
       if ((e = prep_once<K>(XS::SMEM)) != cudaSuccess) return e;
       const dim3 gr = grid_xs<K>(rg, batch, &w);
       K<<<gr, XNT, XS::SMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
@@ -211,10 +212,15 @@ struct Launch {
       return cudaGetLastError();
     }
     const dim3 gr = grid_x(rg, batch, &w);
-    if ((e = prep_once<k_xw_inv_rho<N>>(XSMEM)) != cudaSuccess) return e;
-    k_xw_inv_rho<N><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
+    if ((e = prep_once<k_xw_inv_rho<N, CEN>>(XSMEM)) != cudaSuccess) return e;
+    k_xw_inv_rho<N, CEN><<<gr, XNT, XSMEM, st>>>(psi, H, rg, hpitch, hbstride, tw, a, w);
     ++tl_kernel_launches;
     return cudaGetLastError();
+  }
+  static cudaError_t x_inv_rho(float2* psi, float2* H, const RowGeom& rg, long long hpitch, long long hbstride,
+                               const float4* tw, const RhoArgs& a, int batch, cudaStream_t st) {
+    return a.centre ? x_inv_rho_t<true>(psi, H, rg, hpitch, hbstride, tw, a, batch, st)
+                    : x_inv_rho_t<false>(psi, H, rg, hpitch, hbstride, tw, a, batch, st);
   }
   template <bool FWD>
   static cudaError_t x_kick_t(const float2* psi_in, float2* psi, const float2* H, const RowGeom& rg, long long hpitch,

@@ -510,12 +510,9 @@ struct KickArgs {
   int precise;           // reduce the phase modulo 2 pi in float-float before sincos
   int* err = nullptr;    // error word of abandoned waits of the staged pass (may be null)
   // Frame of the tide (used when tidal != 0): null keeps 1/2 x^T T x about the
-  // box centre.  Otherwise the words the last density pass left per batch
-  // item (CentreWords) give the density maximum x_c and the density's first
-  // moments; centre_mode 1 subtracts the tide's value at x_c, centre_mode 2
-  // its value and gradient there (see tide_frame).
-  const unsigned long long* centre = nullptr;
-  int centre_mode = 0;
+  // box centre; otherwise 4 floats per batch item, the coordinates of cell 0
+  // in the tide's frame and a constant added to the tide (tide_frame_of).
+  const float* frame = nullptr;
 };
 
 // Per-batch-item words a density pass accumulates for the tide frame: [0] the
@@ -525,6 +522,46 @@ struct KickArgs {
 // item (i, j, k the cell indices along x, y, z).  rho = |psi|^2, without the
 // baryon density.  Zeroed before every density pass that fills them.
 enum { CENTRE_WORDS = 5 };
+
+// The tide's frame for one batch item from the words of the last density pass
+// (CentreWords) and its tidal tensor T6.  x_c is the centre of the cell of the
+// density maximum and <x> the density-weighted mean position; for the
+// quadratic tide Phi(x) = 1/2 x^T T x:
+//   mode 1: Phi(x) - Phi(x_c), the potential src/physics/tidal_fields.jl:114
+//     leaves (its gradient cancellation, :115 and :126-146, rebinds the
+//     function's local argument and does not change the caller's potential);
+//   mode 2: Phi(x) - Phi(x_c) - grad Phi(x_c).(x - <x>), what that
+//     cancellation computes: = 1/2 (x - x_c)^T T (x - x_c) + (T x_c).(<x> - x_c).
+// out: the coordinates of cell 0 in the frame (x0, y0, z0) and the constant,
+// from FP64 arithmetic; x0, d: cell 0's coordinates and the spacings.
+__device__ inline void tide_frame_of(float* out, const float* T6, const unsigned long long* w, int mode, int nx,
+                                     int ny, const double* x0, const double* d) {
+  const unsigned flat = 0xffffffffu - (unsigned)(w[0] & 0xffffffffull);
+  const unsigned ix = flat % (unsigned)nx, iy = (flat / (unsigned)nx) % (unsigned)ny;
+  const unsigned iz = flat / ((unsigned)nx * (unsigned)ny);
+  const double xc = x0[0] + d[0] * ix, yc = x0[1] + d[1] * iy, zc = x0[2] + d[2] * iz;
+  const double txx = T6[0], tyy = T6[1], tzz = T6[2], txy = T6[3], txz = T6[4], tyz = T6[5];
+  const double gx = txx * xc + txy * yc + txz * zc;
+  const double gy = txy * xc + tyy * yc + tyz * zc;
+  const double gz = txz * xc + tyz * yc + tzz * zc;
+  if (mode == 1) {
+    out[0] = (float)x0[0];
+    out[1] = (float)x0[1];
+    out[2] = (float)x0[2];
+    out[3] = (float)(-0.5 * (xc * gx + yc * gy + zc * gz));
+    return;
+  }
+  const double s0 = __longlong_as_double((long long)w[1]);
+  const double inv = s0 > 0.0 ? 1.0 / s0 : 0.0;
+  const double mx = x0[0] + d[0] * (__longlong_as_double((long long)w[2]) * inv);
+  const double my = x0[1] + d[1] * (__longlong_as_double((long long)w[3]) * inv);
+  const double mz = x0[2] + d[2] * (__longlong_as_double((long long)w[4]) * inv);
+  out[0] = (float)(-d[0] * ix);
+  out[1] = (float)(-d[1] * iy);
+  out[2] = (float)(-d[2] * iz);
+  out[3] = (float)(gx * (mx - xc) + gy * (my - yc) + gz * (mz - zc));
+}
+
 
 // psi * exp(-i dt pot).
 // Plain form: one FP32 sincos of pot*dt.

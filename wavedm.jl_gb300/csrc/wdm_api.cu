@@ -142,6 +142,7 @@ struct wdm_ctx {
   // leave for it ([batch][CENTRE_WORDS], allocated when a frame is chosen)
   int tide_centre = 0;
   unsigned long long* centre = nullptr;
+  float* frame = nullptr;           // [batch][4] the tide's frame of the next kick
   int* flag = nullptr;              // device words: [0] non-finite psi, [1] abandoned-wait bits
   float* scratch_f = nullptr;       // float field scratch [batch][ncell]
   float2* scratch_h = nullptr;      // half-spectrum scratch
@@ -583,10 +584,7 @@ static KickArgs kick_args(const wdm_ctx* c, double dt, int sched_row) {
   a.v_bstride = c->ncell;
   a.precise = c->d.phase_mode == WDM_PHASE_PRECISE;
   a.err = c->flag + 1;
-  if (c->tide_centre && a.tidal) {
-    a.centre = c->centre;
-    a.centre_mode = c->tide_centre;
-  }
+  if (c->tide_centre && a.tidal) a.frame = c->frame;
   return a;
 }
 
@@ -619,9 +617,17 @@ static wdm_status check_tide_rows(wdm_ctx* c, double t0, double dt, int nkicks, 
   return WDM_OK;
 }
 
-// Kick of psi (in place), or of psi_in into c->psi when psi_in is given.
+// Kick of psi (in place), or of psi_in into c->psi when psi_in is given.  A
+// tide anchored at the density maximum first gets its frame from the words of
+// the last density pass.
 static wdm_status kick(wdm_ctx* c, double dt, int sched_row, bool fwd, const float2* psi_in = nullptr) {
   KickArgs a = kick_args(c, dt, sched_row);
+  if (a.frame) {
+    cudaError_t e = counted(c, [&] {
+      return launch_tide_frame(c->centre, a, c->tide_centre, c->d.nx, c->d.ny, c->d.batch, c->frame, c->st);
+    });
+    if (e != cudaSuccess) return cuda_fail(c, e, "tide frame");
+  }
   const float2* in = psi_in ? psi_in : c->psi;
   cudaError_t e = run_pass(c, fwd ? P_KICK_FWD : P_KICK, [&] {
     return c->kx->x_kick(in, c->psi, c->H, rows_psi(c, LP_X_KICK), c->hpitch, c->nhalf, c->twx, a, fwd, c->d.batch, c->st);
@@ -740,7 +746,7 @@ wdm_status wdm_destroy(wdm_ctx* c) {
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
   for (void* p : bufs)
     if (p) cudaFree(p);
-  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc, c->diag_wsum, c->diag_wmin, c->centre};
+  void* adj[] = {c->lam, c->Hmu, c->rho_t, c->D6, c->adj_acc, c->diag_wsum, c->diag_wmin, c->centre, c->frame};
   for (void* p : adj)
     if (p) cudaFree(p);
   for (auto* v : {&c->ck_psi, &c->ck_H, &c->slot_psi, &c->slot_H, &c->slot2_psi, &c->slot2_H})
@@ -1087,6 +1093,7 @@ wdm_status wdm_set_tidal_centering(wdm_ctx* c, int32_t mode) {
   if (mode != WDM_TIDE_BOX_CENTRE && mode != WDM_TIDE_REFERENCE && mode != WDM_TIDE_DENSITY_MAX)
     return fail(c, WDM_ERR_INVALID, "wdm_set_tidal_centering: unknown mode");
   if (mode != WDM_TIDE_BOX_CENTRE && !c->centre) {
+    WDM_TRY(dalloc(c, &c->frame, (size_t)4 * c->d.batch));
     WDM_TRY(dalloc(c, &c->centre, (size_t)CENTRE_WORDS * c->d.batch));
     WDM_CU(c, cudaMemsetAsync(c->centre, 0, sizeof(unsigned long long) * CENTRE_WORDS * c->d.batch, c->st));
     WDM_CU(c, cudaStreamSynchronize(c->st));
@@ -1947,6 +1954,8 @@ static wdm_status build_members(wdm_group* g, const std::vector<double>& dt, int
     ra.shift = c->shift;
     ra.err = c->flag + 1;
     e.centre = (c->tide_centre && c->tide_on) ? c->centre : nullptr;
+    e.frame = e.centre ? c->frame : nullptr;
+    e.centre_mode = c->tide_centre;
     ra.centre = e.centre;
     e.rho = ra;
     DriftOp op{};
@@ -2011,6 +2020,13 @@ static wdm_status group_launch(wdm_group* g, int32_t nsteps, const std::vector<d
       wdm_ctx* c0 = g->m[0];
       const long long l0 = tl_kernel_launches;
       e = cudaMemsetAsync(g->dwords, 0, sizeof(unsigned) * ENS_SYNC_WORDS, g->st);
+      // the frames of the first kicks (later ones are made inside the launch)
+      for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+        wdm_ctx* c = g->m[i];
+        if (c->tide_centre && c->tide_on)
+          e = launch_tide_frame(c->centre, kick_args(c, dt[i], 0), c->tide_centre, c->d.nx, c->d.ny, c->d.batch,
+                                c->frame, g->st);
+      }
       if (e == cudaSuccess)
         e = ens_launch(g->dmem, (int)n, nsteps, mode, g->dwords, c0->flag + 1, g->ens_smem, g->ens_grid, g->st);
       launches = tl_kernel_launches - l0;

@@ -124,7 +124,6 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
           long long hbstride, const float4* __restrict__ twg, KickArgs a, XWork w) {
   WDM_XPASS_PROLOGUE
   WDM_XSTAGE_PROLOGUE
-  using Rev = typename Reverse<Rad>::type;
   auto issue_h = [&](long long u) {
     int b, ra;
     unit_rows(u, C::GROUPS, ppi, &b, &ra);
@@ -150,13 +149,13 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
     ra += 2 * g;  // this lane group's pair
     if (!WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
     float2 v[N / T];
-    load_packed_half<N, T, RadInfo<Rev>::first>(v, slotA + (2 * g) * S::H_P, slotA + (2 * g + 1) * S::H_P, true, t);
+    load_packed_half<N, T, R1>(v, slotA + (2 * g) * S::H_P, slotA + (2 * g + 1) * S::H_P, true, t);
     xrelease();
     if (un < nunits) {
       if (lane == 0) issue_h(un);
       pend |= 1u;
     }
-    run_wstages<N, T, C::NP, true>(Rev{}, v, buf, twr, t);  // ends with radix R1
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // ends with radix RS
     float phi[2][N / T];
 #pragma unroll
     for (int q = 0; q < N / T; ++q) {
@@ -186,9 +185,9 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       for (int half = 0; half < 2; ++half) {
         const float2* srow = slotB + (2 * g + half) * S::PSI_P;
 #pragma unroll
-        for (int i = 0; i < N / (R1 * T); ++i)
+        for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-          for (int k = 0; k < R1; ++k) v[i * R1 + k] = srow[slot_pos<N, T, R1>(t, i, k)];
+          for (int k = 0; k < RS; ++k) v[i * RS + k] = srow[slot_pos<N, T, RS>(t, i, k)];
         if (half == 1) release_b();
         const int r = ra + half;
         kick_row<N, true>(v, phr, T6, a, rg, r, b, true, psi + b * rg.bstride + (long long)r * rg.pitch, buf, tw, t);
@@ -202,24 +201,25 @@ k_xs_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
       float2 vb[N / T];
       const float2* sb = slotB + (2 * g) * S::PSI_P;
 #pragma unroll
-      for (int i = 0; i < N / (R1 * T); ++i)
+      for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-        for (int k = 0; k < R1; ++k) {
-          v[i * R1 + k] = sb[slot_pos<N, T, R1>(t, i, k)];
-          vb[i * R1 + k] = sb[S::PSI_P + slot_pos<N, T, R1>(t, i, k)];
+        for (int k = 0; k < RS; ++k) {
+          v[i * RS + k] = sb[slot_pos<N, T, RS>(t, i, k)];
+          vb[i * RS + k] = sb[S::PSI_P + slot_pos<N, T, RS>(t, i, k)];
         }
       release_b();
-      kick_points<N>(v, phi[0], T6, a, rg, ra, b, true, t);
-      kick_points<N>(vb, phi[1], T6, a, rg, ra + 1, b, true, t);
+      kick_points<N, RS>(v, phi[0], T6, a, rg, ra, b, true, t);
+      kick_points<N, RS>(vb, phi[1], T6, a, rg, ra + 1, b, true, t);
       float2* rowa = psi + b * rg.bstride + (long long)ra * rg.pitch;
-      store_row<N, R1>(rowa, v, true, t);
-      store_row<N, R1>(rowa + rg.pitch, vb, true, t);
+      store_row<N, RS>(rowa, v, true, t);
+      store_row<N, RS>(rowa + rg.pitch, vb, true, t);
     }
   }
 }
 
-// P5 (staged): psi x-inverse (+mask), rho = |psi|^2 (+rho_b) - shift, packed R2C -> H.
-template <int N>
+// P5 (staged): psi x-inverse (+mask), rho = |psi|^2 (+rho_b) - shift, packed R2C -> H
+// (CEN: with the density maximum and moments for the tide's frame).
+template <int N, bool CEN>
 __global__ void __launch_bounds__(XCfg<N>::NT, XStage<N>::MINB)
 k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
              const float4* __restrict__ twg, RhoArgs a, XWork w) {
@@ -313,8 +313,8 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       release_p();
       if (with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
       float2* rowa = psi + b * rg.bstride + (long long)ra * rg.pitch;
-      rho_row_post<N>(v, a, rg, ra, true, rowa, rb_of(0), shift, 0, rho0, z, t, ca);
-      rho_row_post<N>(vb, a, rg, ra + 1, true, rowa + rg.pitch, rb_of(1), shift, 1, rho0, z, t, ca);
+      rho_row_post<N, CEN>(v, a, rg, ra, true, rowa, rb_of(0), shift, 0, rho0, z, t, ca);
+      rho_row_post<N, CEN>(vb, a, rg, ra + 1, true, rowa + rg.pitch, rb_of(1), shift, 1, rho0, z, t, ca);
       if (with_rb) release_r();
     } else {
 #pragma unroll
@@ -334,12 +334,12 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
       if (half == 1) release_p();
       if (half == 0 && with_rb && !WDM_XSTAGE_WAIT(0)) WDM_XSTAGE_FAIL(a.err);
       const int r = ra + half;
-      inv_rho_row<N>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb_of(half), shift, half,
-                     rho0, z, buf, tw, t, ca);
+      inv_rho_row<N, CEN>(v, a, rg, r, true, psi + b * rg.bstride + (long long)r * rg.pitch, rb_of(half), shift,
+                          half, rho0, z, buf, tw, t, ca);
       if (half == 1 && with_rb) release_r();
     }
     }
-    if (a.centre) centre_pair_done<N>(a, rg, ca, cs, b, ra, true, t);
+    if constexpr (CEN) centre_pair_done<N>(a, rg, ca, cs, b, ra, true, t);
     if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t, (mcur >> (2 * g)) & 3u);
     mcur = mnext;
     reorder<N, T, RS, R1>(z, v);
@@ -347,7 +347,7 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     float2* hrow = H + b * hbstride + ra * hpitch;
     store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, true, t);
   }
-  if (a.centre && t == 0) cs.flush(a.centre);
+  if (CEN && t == 0) cs.flush(a.centre);
 }
 
 // Adjoint kick (staged): the arithmetic of k_xw_adj_kick, with the H rows in

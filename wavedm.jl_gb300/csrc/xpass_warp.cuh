@@ -188,14 +188,14 @@ struct XPlan<256> {
   static constexpr int N = 256, T = 32;
   using Fwd = Radices<8, 8, 4>;
 };
+// 384 = 4 4 4 6: the strides NS = 1, 4, 16, 64 of the stages are powers of two,
+// so each lane's exchange addresses (j / NS, j % NS of j = t + 32 i) cost
+// shifts and masks; the order 6 4 4 4 (NS = 1, 6, 24, 96) costs a division by
+// a constant per point and exchange, and measured 8% slower in the density pass.
 template <>
 struct XPlan<384> {
   static constexpr int N = 384, T = 32;
-#if defined(WDM_X384_FWD_4446)
   using Fwd = Radices<4, 4, 4, 6>;
-#else
-  using Fwd = Radices<6, 4, 4, 4>;
-#endif
 };
 
 template <int N>
@@ -206,7 +206,12 @@ struct XCfg {
   static constexpr int WARPS = 4;                      // warps per CTA
   static constexpr int NT = 32 * WARPS;
   static constexpr int NP = N + N / 4 + 1;             // padded exchange buffer per group
-  static constexpr size_t SMEM = sizeof(float4) * 2 * N + sizeof(float2) * (size_t)NP * GROUPS * WARPS;
+#if defined(WDM_XTW_GLOBAL)
+  static constexpr size_t TW_BYTES = 0;  // twiddles read from global memory (L1), not staged
+#else
+  static constexpr size_t TW_BYTES = sizeof(float4) * N;  // the forward-order table (both directions)
+#endif
+  static constexpr size_t SMEM = TW_BYTES + sizeof(float2) * (size_t)NP * GROUPS * WARPS;
 };
 
 // Work distribution: warp-units of GROUPS row pairs, grid-stride over all
@@ -264,6 +269,18 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
     }
 }
 
+// The x twiddle table of the forward radix order (N entries), which every
+// x-pass transform uses in both directions: staged in shared memory, or
+// (WDM_XTW_GLOBAL, a tuning variant) read through L1 from global memory.
+#if defined(WDM_XTW_GLOBAL)
+#define WDM_XPASS_TWIDDLES const float4* tw = twg + TW_X_FWD * N;
+#else
+#define WDM_XPASS_TWIDDLES                                   \
+  float4* tw = reinterpret_cast<float4*>(smem);              \
+  load_twiddles(tw, twg + TW_X_FWD * N, N);                  \
+  __syncthreads();
+#endif
+
 #define WDM_XPASS_PROLOGUE                                                          \
   using C = XCfg<N>;                                                                \
   constexpr int T = C::T;                                                           \
@@ -272,28 +289,24 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
   (void)R1;                                                                         \
   (void)RS;                                                                         \
   extern __shared__ float2 smem[];                                                  \
-  float4* tw = reinterpret_cast<float4*>(smem); /* [x fwd | x rev] tables */      \
-  const float4* twr = tw + N;                                                       \
-  (void)twr;                                                                        \
-  load_twiddles(tw, twg + TW_X_FWD * N, 2 * N);                                     \
-  __syncthreads();                                                                  \
+  WDM_XPASS_TWIDDLES                                                                \
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;                       \
   const int g = lane / T, t = lane % T;                                             \
-  float2* buf = smem + 4 * N + (size_t)(warp * C::GROUPS + g) * C::NP;              \
+  float2* buf = smem + C::TW_BYTES / sizeof(float2) + (size_t)(warp * C::GROUPS + g) * C::NP; \
   const long long nunits = w.units(C::GROUPS);                                      \
   const long long wstride = (long long)gridDim.x * C::WARPS;
 
 // ----------------------------------------------------------------------------
 // P1: Phi rows from H (C2R of the packed pair), kick, forward x-FFT (or not)
 // ----------------------------------------------------------------------------
-// The kick of one row: v holds psi row r at radix-R1 slots, phi its potential
-// at the same slots; v <- v exp(-i dt pot).
-template <int N>
+// The kick of one row: v holds psi row r at radix-R slots (R: the last radix
+// of the x plan, where the potential's C2R leaves it), phi its potential at the
+// same slots; v <- v exp(-i dt pot).
+template <int N, int R1 = RadInfo<typename XPlan<N>::Fwd>::last>
 __device__ __forceinline__ void kick_points(float2* v, const float* phi, const float* T6, const KickArgs& a,
                                             const RowGeom& rg, int r, int b, bool ok, int t) {
   using C = XCfg<N>;
   constexpr int T = C::T;
-  constexpr int R1 = RadInfo<typename XPlan<N>::Fwd>::first;
   const float* vrow = a.V ? a.V + b * a.v_bstride + (long long)r * rg.pitch : nullptr;
   const int y = r % rg.ny, z = r / rg.ny;
   // coordinates in the tide's frame (T6[6..8]: cell 0's, T6[9]: constant)
@@ -329,8 +342,10 @@ __device__ __forceinline__ void store_row(float2* row, const float2* v, bool ok,
     for (int k = 0; k < R; ++k) row[slot_pos<N, T, R>(t, i, k)] = v[i * R + k];
 }
 
-// One row of the kick pass: kick, then (FWD) the forward x transform, and
-// store to `row` (when ok).  Used by the direct kernel.
+// One row of the kick pass: v holds psi row r at radix-RS slots (where the
+// potential's C2R leaves phi); kick, then (FWD) the forward x transform, whose
+// first stage wants radix-R1 slots (a renaming of the same registers), and
+// store to `row` (when ok).
 template <int N, bool FWD>
 __device__ __forceinline__ void kick_row(float2* v, const float* phi, const float* T6, const KickArgs& a,
                                          const RowGeom& rg, int r, int b, bool ok, float2* row, float2* buf,
@@ -339,62 +354,32 @@ __device__ __forceinline__ void kick_row(float2* v, const float* phi, const floa
   constexpr int T = C::T;
   using Rad = typename XPlan<N>::Fwd;
   constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
-  kick_points<N>(v, phi, T6, a, rg, r, b, ok, t);
+  kick_points<N, RS>(v, phi, T6, a, rg, r, b, ok, t);
   if constexpr (FWD) {
-    run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
-    store_row<N, RS>(row, v, ok, t);
+    float2 w[N / T];
+    reorder<N, T, RS, R1>(v, w);
+    run_wstages<N, T, C::NP, false>(Rad{}, w, buf, tw, t);
+    store_row<N, RS>(row, w, ok, t);
   } else {
-    store_row<N, R1>(row, v, ok, t);
+    store_row<N, RS>(row, v, ok, t);
   }
-}
-
-// The tide's frame for batch item b from the words of the last density pass
-// (CentreWords).  x_c is the centre of the cell of the density maximum and
-// <x> the density-weighted mean position; for the quadratic tide
-// Phi(x) = 1/2 x^T T x:
-//   centre_mode 1: Phi(x) - Phi(x_c), the potential src/physics/tidal_fields.jl:114
-//     leaves (its gradient cancellation, :115 and :126-146, rebinds the
-//     function's local argument and does not change the caller's potential);
-//   centre_mode 2: Phi(x) - Phi(x_c) - grad Phi(x_c).(x - <x>), what that
-//     cancellation computes: = 1/2 (x - x_c)^T T (x - x_c) + (T x_c).(<x> - x_c).
-// Writes the frame's cell-0 coordinates to f[6..8] and the constant to f[9];
-// the arithmetic is FP64, once per unit of rows.
-static __device__ __noinline__ void tide_frame(float* f, const KickArgs& a, int nx, int ny, int b) {
-  const unsigned long long* w = a.centre + (long long)CENTRE_WORDS * b;
-  const unsigned flat = 0xffffffffu - (unsigned)(w[0] & 0xffffffffull);
-  const unsigned ix = flat % (unsigned)nx, iy = (flat / (unsigned)nx) % (unsigned)ny;
-  const unsigned iz = flat / ((unsigned)nx * (unsigned)ny);
-  const double xc = a.x0 + (double)a.dx * ix, yc = a.y0 + (double)a.dy * iy, zc = a.z0 + (double)a.dz * iz;
-  const double txx = f[0], tyy = f[1], tzz = f[2], txy = f[3], txz = f[4], tyz = f[5];
-  const double gx = txx * xc + txy * yc + txz * zc;
-  const double gy = txy * xc + tyy * yc + tyz * zc;
-  const double gz = txz * xc + tyz * yc + tzz * zc;
-  if (a.centre_mode == 1) {
-    f[9] = (float)(-0.5 * (xc * gx + yc * gy + zc * gz));
-    return;
-  }
-  const double s0 = __longlong_as_double((long long)w[1]);
-  const double inv = s0 > 0.0 ? 1.0 / s0 : 0.0;
-  const double mx = a.x0 + (double)a.dx * (__longlong_as_double((long long)w[2]) * inv);
-  const double my = a.y0 + (double)a.dy * (__longlong_as_double((long long)w[3]) * inv);
-  const double mz = a.z0 + (double)a.dz * (__longlong_as_double((long long)w[4]) * inv);
-  f[6] = (float)(-(double)a.dx * ix);
-  f[7] = (float)(-(double)a.dy * iy);
-  f[8] = (float)(-(double)a.dz * iz);
-  f[9] = (float)(gx * (mx - xc) + gy * (my - yc) + gz * (mz - zc));
 }
 
 // Tidal tensor of batch item b in T6[0..5] and the tide's frame in T6[6..9]
 // (cell-0 coordinates and a constant; the box centre and 0 without a frame).
 template <int N>
-__device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, const RowGeom& rg, int b) {
+__device__ __forceinline__ void kick_tidal(float* T6, const KickArgs& a, const RowGeom&, int b) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) T6[q] = a.T6b ? a.T6b[b * 6 + q] : a.T6[q];
-  T6[6] = a.x0;
-  T6[7] = a.y0;
-  T6[8] = a.z0;
-  T6[9] = 0.f;
-  if (a.centre && a.tidal) tide_frame(T6, a, N, rg.ny, b);
+  if (a.frame) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) T6[6 + q] = a.frame[4 * b + q];
+  } else {
+    T6[6] = a.x0;
+    T6[7] = a.y0;
+    T6[8] = a.z0;
+    T6[9] = 0.f;
+  }
 }
 
 // Density maximum and first moments of one row pair, per lane (CentreWords).
@@ -522,11 +507,9 @@ __device__ __forceinline__ void xw_kick_units(const float2* psi_in, float2* psi,
   using C = XCfg<N>;
   constexpr int T = C::T;
   using Rad = typename XPlan<N>::Fwd;
-  using Rev = typename Reverse<Rad>::type;
-  constexpr int R1 = RadInfo<Rad>::first;
+  constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
   const int lane = threadIdx.x & 31, g = lane / T, t = lane % T;
   const float4* tw = sl.tw;
-  const float4* twr = tw + N;
   float2* buf = sl.buf;
   const long long nunits = w.units(C::GROUPS);
   for (long long u = sl.u0; u < nunits; u += sl.ustride) {
@@ -536,8 +519,8 @@ __device__ __forceinline__ void xw_kick_units(const float2* psi_in, float2* psi,
     const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
     const float2* hrow = H + b * hbstride + ra * hpitch;
     float2 v[N / T];
-    load_packed_half<N, T, RadInfo<Rev>::first>(v, hrow, hrow + hpitch, ok, t);
-    run_wstages<N, T, C::NP, true>(Rev{}, v, buf, twr, t);  // ends with radix R1
+    load_packed_half<N, T, R1>(v, hrow, hrow + hpitch, ok, t);
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);  // ends with radix RS
     float phi[2][N / T];
 #pragma unroll
     for (int q = 0; q < N / T; ++q) {
@@ -551,9 +534,9 @@ __device__ __forceinline__ void xw_kick_units(const float2* psi_in, float2* psi,
       const int r = ra + half;
       const float2* irow = psi_in + b * rg.bstride + (long long)r * rg.pitch;
 #pragma unroll
-      for (int i = 0; i < N / (R1 * T); ++i)
+      for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-        for (int k = 0; k < R1; ++k) v[i * R1 + k] = ok ? irow[slot_pos<N, T, R1>(t, i, k)] : make_float2(0.f, 0.f);
+        for (int k = 0; k < RS; ++k) v[i * RS + k] = ok ? irow[slot_pos<N, T, RS>(t, i, k)] : make_float2(0.f, 0.f);
       kick_row<N, FWD>(v, phi[half], T6, a, rg, r, b, ok, psi + b * rg.bstride + (long long)r * rg.pitch, buf, tw, t);
     }
   }
@@ -578,7 +561,7 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
 // space at radix-RS slots; mask it and store it back to `row` (write_psi), then
 // form rho - shift into rho0 (half 0) or the packed z (half 1).  rb: the
 // baryon density row or null.
-template <int N>
+template <int N, bool CEN>
 __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
                                              float2* row, const float* rb, float shift, int half, float* rho0,
                                              float2* z, int t, CentreAcc& ca) {
@@ -602,7 +585,7 @@ __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const 
       const float2 q = v[i * RS + k];
       float d = q.x * q.x + q.y * q.y;
       if (ok && a.nonfinite && !isfinite(d)) *a.nonfinite = 1;
-      if (a.centre) {
+      if constexpr (CEN) {
         const int x = slot_pos<N, T, RS>(t, i, k);
         ca.add(d, (unsigned)r * (unsigned)N + (unsigned)x, x, half);
       }
@@ -615,16 +598,16 @@ __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const 
 // One row of P5: v holds psi row r (write_psi: x-spectral at radix-R1 slots,
 // else real space at radix-RS slots).  Inverts it (write_psi), then
 // rho_row_post.
-template <int N>
+template <int N, bool CEN>
 __device__ __forceinline__ void inv_rho_row(float2* v, const RhoArgs& a, const RowGeom& rg, int r, bool ok,
                                             float2* row, const float* rb, float shift, int half, float* rho0,
                                             float2* z, float2* buf, const float4* tw, int t, CentreAcc& ca) {
   using C = XCfg<N>;
   if (a.write_psi) run_wstages<N, C::T, C::NP, true>(typename XPlan<N>::Fwd{}, v, buf, tw, t);
-  rho_row_post<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, t, ca);
+  rho_row_post<N, CEN>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, t, ca);
 }
 
-template <int N>
+template <int N, bool CEN>
 __device__ __forceinline__ void xw_inv_rho_units(float2* __restrict__ psi, float2* __restrict__ H, const RowGeom& rg,
                                                  long long hpitch, long long hbstride, const RhoArgs& a,
                                                  const XWork& w, const XSlice& sl) {
@@ -666,9 +649,9 @@ __device__ __forceinline__ void xw_inv_rho_units(float2* __restrict__ psi, float
       }
       const bool rb_row = a.rho_b && (!a.rb_rows || a.rb_rows[r]);  // rows without baryon mass are zero
       const float* rb = rb_row ? a.rho_b + b * a.rb_bstride + (long long)r * rg.pitch : nullptr;
-      inv_rho_row<N>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t, ca);
+      inv_rho_row<N, CEN>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t, ca);
     }
-    if (a.centre) centre_pair_done<N>(a, rg, ca, cs, b, ra, ok, t);
+    if constexpr (CEN) centre_pair_done<N>(a, rg, ca, cs, b, ra, ok, t);
     if (a.rb_zero) {
       const unsigned fl = ok ? (!a.rb_rows ? 3u : (a.rb_rows[ra] ? 1u : 0u) | (a.rb_rows[ra + 1] ? 2u : 0u)) : 0u;
       clear_rb_pair<N>(a, rg, b, ra, ok, t, fl);
@@ -678,17 +661,20 @@ __device__ __forceinline__ void xw_inv_rho_units(float2* __restrict__ psi, float
     float2* hrow = H + b * hbstride + ra * hpitch;
     store_packed_half<N, T, RS>(v, buf, hrow, hrow + hpitch, ok, t);
   }
-  if (a.centre && t == 0) cs.flush(a.centre);
+  if (CEN && t == 0) cs.flush(a.centre);
 }
 
-template <int N>
+// CEN: also accumulate the density maximum and moments for the tide's frame
+// (RhoArgs::centre), a compile-time choice so that the pass without it keeps
+// its registers and instructions.
+template <int N, bool CEN>
 __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long long hpitch, long long hbstride,
              const float4* __restrict__ twg, RhoArgs a, XWork w) {
   WDM_XPASS_PROLOGUE
   (void)nunits;
-  xw_inv_rho_units<N>(psi, H, rg, hpitch, hbstride, a, w,
-                      XSlice{(long long)blockIdx.x * C::WARPS + warp, wstride, tw, buf});
+  xw_inv_rho_units<N, CEN>(psi, H, rg, hpitch, hbstride, a, w,
+                           XSlice{(long long)blockIdx.x * C::WARPS + warp, wstride, tw, buf});
 }
 
 // Plain C2C x pass (rows processed pairwise, scaled output).
@@ -725,7 +711,6 @@ __global__ void __launch_bounds__(XCfg<N>::NT, WDM_X_MINB)
 k_xw_c2r(const float2* __restrict__ H, float* __restrict__ out, RowGeom rg, long long hpitch, long long hbstride,
          const float4* __restrict__ twg, XWork w) {
   WDM_XPASS_PROLOGUE
-  using Rev = typename Reverse<Rad>::type;
   for (long long u = (long long)blockIdx.x * C::WARPS + warp; u < nunits; u += wstride) {
     const long long pp = u * C::GROUPS + g;
     const bool ok = pp < (long long)w.pairs_per_item * w.batch;
@@ -733,17 +718,17 @@ k_xw_c2r(const float2* __restrict__ H, float* __restrict__ out, RowGeom rg, long
     const int ra = ok ? 2 * (int)(pp - (long long)b * w.pairs_per_item) : 0;
     const float2* hrow = H + b * hbstride + ra * hpitch;
     float2 v[N / T];
-    load_packed_half<N, T, RadInfo<Rev>::first>(v, hrow, hrow + hpitch, ok, t);
-    run_wstages<N, T, C::NP, true>(Rev{}, v, buf, twr, t);
+    load_packed_half<N, T, R1>(v, hrow, hrow + hpitch, ok, t);
+    run_wstages<N, T, C::NP, true>(Rad{}, v, buf, tw, t);
     if (!ok) continue;
     float* oa = out + b * rg.bstride + (long long)ra * rg.pitch;
 #pragma unroll
-    for (int i = 0; i < N / (R1 * T); ++i)
+    for (int i = 0; i < N / (RS * T); ++i)
 #pragma unroll
-      for (int k = 0; k < R1; ++k) {
-        const int x = slot_pos<N, T, R1>(t, i, k);
-        oa[x] = v[i * R1 + k].x;
-        oa[rg.pitch + x] = v[i * R1 + k].y;
+      for (int k = 0; k < RS; ++k) {
+        const int x = slot_pos<N, T, RS>(t, i, k);
+        oa[x] = v[i * RS + k].x;
+        oa[rg.pitch + x] = v[i * RS + k].y;
       }
   }
 }
