@@ -194,8 +194,14 @@ struct XPlan<256> {
 // a constant per point and exchange, and measured 8% slower in the density pass.
 template <>
 struct XPlan<384> {
+#if defined(WDM_X384_T16)
+  // tuning variant: 16 lanes per row, 24 points per lane, two exchanges
+  static constexpr int N = 384, T = 16;
+  using Fwd = Radices<8, 8, 6>;
+#else
   static constexpr int N = 384, T = 32;
   using Fwd = Radices<4, 4, 4, 6>;
+#endif
 };
 
 template <int N>
