@@ -198,6 +198,10 @@ struct XPlan<384> {
   // tuning variant: 16 lanes per row, 24 points per lane, two exchanges
   static constexpr int N = 384, T = 16;
   using Fwd = Radices<8, 8, 6>;
+#elif defined(WDM_X384_ORDER_6444)
+  // the order 6 4 4 4, for comparison
+  static constexpr int N = 384, T = 32;
+  using Fwd = Radices<6, 4, 4, 4>;
 #else
   static constexpr int N = 384, T = 32;
   using Fwd = Radices<4, 4, 4, 6>;
