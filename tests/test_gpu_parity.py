@@ -393,25 +393,31 @@ def test_precise_phases_conserve_mass(wdm, n, c, steps):
 def test_forward_transform_keeps_energy_of_smooth_lines_at_384(wdm, torch_cuda):
     """Energy of the unnormalised forward 3D transform, sum |F psi|^2 = N sum |psi|^2,
     on 65536 smooth x-lines of length 384 (a soliton profile with random centre,
-    width and phase per line, as the rows of a halo): the mean relative error
-    must stay at the rounding noise (~1e-10 here).  The stages of the 384-point
-    x plan that hold twiddles with a component of exactly +-1/2 lost their FP32
-    correction before the twiddle rule was fixed, which biased this energy by
-    about -1e-9 per transform and drifted the 384^3 mass by -3e-6 over 2000 steps."""
+    width and phase per line, as the rows of a halo), averaged over four draws.
+    One draw's relative error is rounding noise of about 4e-10 (measured on both
+    radix orders of the 384-point x plan); the stages of the x plan that hold
+    twiddles with a component of exactly +-1/2 lost their FP32 correction before
+    the twiddle rule was fixed, which biased every draw by about -1e-9 and drifted
+    the 384^3 mass by -3e-6 over 2000 steps (that drift itself is bounded by
+    tests/test_gpu_workloads.py)."""
     nx, ny, nz = 384, 256, 256
-    rng = np.random.default_rng(12)
-    x = (np.arange(nx) - nx // 2) * (40.0 / 384)
-    c = rng.uniform(-3, 3, (nz, ny, 1))
-    rc = rng.uniform(1.0, 2.0, (nz, ny, 1))
-    amp = 1.0 / (1 + 0.091 * ((x[None, None, :] - c) / rc) ** 2) ** 4
-    ph = 0.1 * rng.standard_normal((nz, ny, nx)) + rng.uniform(0, 2 * np.pi, (nz, ny, 1))
-    psi = (amp * np.exp(1j * ph)).astype(np.complex64)
-    with wdm.SPEContext((nx, ny, nz), (40.0, 40.0 * ny / nx, 40.0 * nz / nx)) as ctx:
-        d = torch_cuda.from_numpy(psi).cuda()
-        out = ctx.fft3d(d).cpu().numpy()
-    e_in = np.sum(np.abs(psi.astype(np.complex128)) ** 2) * (nx * ny * nz)
-    e_out = np.sum(np.abs(out.astype(np.complex128)) ** 2)
-    assert abs(e_out / e_in - 1) < 4e-10
+    errs = []
+    for seed in (12, 13, 14, 15):
+        rng = np.random.default_rng(seed)
+        x = (np.arange(nx) - nx // 2) * (40.0 / 384)
+        c = rng.uniform(-3, 3, (nz, ny, 1))
+        rc = rng.uniform(1.0, 2.0, (nz, ny, 1))
+        amp = 1.0 / (1 + 0.091 * ((x[None, None, :] - c) / rc) ** 2) ** 4
+        ph = 0.1 * rng.standard_normal((nz, ny, nx)) + rng.uniform(0, 2 * np.pi, (nz, ny, 1))
+        psi = (amp * np.exp(1j * ph)).astype(np.complex64)
+        with wdm.SPEContext((nx, ny, nz), (40.0, 40.0 * ny / nx, 40.0 * nz / nx)) as ctx:
+            d = torch_cuda.from_numpy(psi).cuda()
+            out = ctx.fft3d(d).cpu().numpy()
+        e_in = np.sum(np.abs(psi.astype(np.complex128)) ** 2) * (nx * ny * nz)
+        e_out = np.sum(np.abs(out.astype(np.complex128)) ** 2)
+        errs.append(e_out / e_in - 1)
+    assert abs(np.mean(errs)) < 6e-10, errs
+    assert max(abs(e) for e in errs) < 2e-9, errs
 
 
 STEP_X_CASES = [(384, 16, 8), (256, 8, 16), (192, 16, 8), (128, 16, 8), (96, 8, 8), (512, 8, 8)]
