@@ -11,8 +11,9 @@
 // WAIT_MAX_POLLS polls) records WDM_DEVERR_BARRIER, raises the abort word and
 // leaves, and every other CTA leaves at its next barrier, so the launch always
 // ends.  Members keep their buffers; the pass bodies are those of the direct
-// x passes and the register-tile line passes (xw_kick_units, xw_inv_rho_units,
-// lfft_tile_one), so a step equals those launches bit for bit.
+// x passes and of the line passes (xw_kick_units, xw_inv_rho_units, and
+// lfft_pipe_run, which prefetches tiles by cp.async), all with the arithmetic of
+// the per-pass launches, so a step equals those launches bit for bit.
 #include "ensemble.cuh"
 
 #include <algorithm>
@@ -79,7 +80,7 @@ constexpr size_t x_smem() {
 
 template <int N, int NTAB>
 constexpr size_t line_smem() {
-  return sizeof(float2) * (2 * (size_t)NTAB * N + (size_t)(ENS_THREADS / threads_for<N>()) * N * LPITCH);
+  return sizeof(float2) * (2 * (size_t)NTAB * N + (size_t)(ENS_THREADS / threads_for<N>()) * 2 * N * LBUF);
 }
 
 template <int N, bool FWD>
@@ -112,7 +113,9 @@ __device__ __noinline__ void x_rho(const EnsMember& m, unsigned char* sm, int vb
 }
 
 // Line pass: the CTA's threads form SUB groups of threads_for<N>() that take
-// SUB consecutive tiles at a time (all groups reach the same barriers).
+// SUB consecutive tiles per round, each group prefetching its next tile by
+// cp.async into its own double buffer (lfft_pipe_run; all groups reach the
+// same barriers).
 template <int N, int MODE, class Op>
 __device__ __noinline__ void lines(float2* data, const LineGeom& g, const float4* twg, const Op& op, int batch,
                                    unsigned char* sm, int vb, int vg) {
@@ -121,18 +124,10 @@ __device__ __noinline__ void lines(float2* data, const LineGeom& g, const float4
   constexpr int SUB = ENS_THREADS / NT;
   static_assert(SUB * NT == ENS_THREADS, "tile groups fill the CTA");
   float4* tw = reinterpret_cast<float4*>(sm);
-  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);  // visible after lfft_tile_one's first barrier
+  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);  // visible after the first round's barrier
   const int sub = threadIdx.x / NT, tid = threadIdx.x % NT;
-  float2* s = reinterpret_cast<float2*>(sm) + 2 * NTAB * N + (size_t)sub * N * LPITCH;
-  const int tpi = (g.nlines + LINES - 1) / LINES;
-  const long long total = (long long)tpi * batch;
-  for (long long t0 = (long long)vb * SUB; t0 < total; t0 += (long long)vg * SUB) {
-    const long long tile = t0 + sub;
-    const bool have = tile < total;
-    const int b = have ? (int)(tile / tpi) : 0;
-    const int line0 = have ? (int)(tile - (long long)b * tpi) * LINES : g.nlines;  // past the end: no line
-    lfft_tile_one<N, MODE, Op>(data, g, tw, op, line0, b, s, tid);
-  }
+  float2* bufs = reinterpret_cast<float2*>(sm) + 2 * NTAB * N + (size_t)sub * 2 * N * LBUF;
+  lfft_pipe_run<N, MODE, Op>(data, g, tw, op, batch, bufs, tid, (long long)vb * SUB, (long long)vg * SUB, sub);
   __syncthreads();
 }
 

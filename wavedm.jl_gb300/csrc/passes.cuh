@@ -207,35 +207,38 @@ __device__ __forceinline__ void lines_issue(float2* buf, const LineGeom& g, floa
   }
 }
 
+// The tiles base + sub, base + step + sub, ... (tile numbers over all batch
+// items) by the threads tid < threads_for<N>() of one group, with the group's
+// double buffer bufs (2 N LBUF entries) and the twiddle tables at tw: the
+// cp.async copy of the group's next tile is in flight while its current one is
+// transformed.  Every thread of the CTA runs the same rounds (a group without
+// a tile in a round computes on stale data and stores nothing), so the CTA's
+// barriers line up; the arithmetic is that of lfft_tile_one.
 template <int N, int MODE, class Op>
-__global__ void __launch_bounds__(threads_for<N>(), min_blocks<N>())
-k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op, int batch) {
+__device__ __forceinline__ void lfft_pipe_run(float2* __restrict__ data, const LineGeom& g, const float4* tw,
+                                              const Op& op, int batch, float2* bufs, int tid, long long base,
+                                              long long step, int sub) {
   using P = Plan<N>;
   constexpr int T = P::T;
   using Rad = typename P::Fwd;
   using Rev = typename Reverse<Rad>::type;
   constexpr int R1 = RadInfo<Rad>::first, RS = RadInfo<Rad>::last;
-  extern __shared__ float2 smem[];
-  float4* tw = reinterpret_cast<float4*>(smem);  // line fwd [| line rev] tables
-  constexpr int NTAB = MODE == 2 ? 2 : 1;
-  float2* bufs = smem + 2 * NTAB * N;
-  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);
-  const int l = threadIdx.x % LINES, t = threadIdx.x / LINES;
+  const int l = tid % LINES, t = tid / LINES;
   const int tiles_per_item = (g.nlines + LINES - 1) / LINES;
   const long long total = (long long)tiles_per_item * batch;
-  long long tile = blockIdx.x;
-  if (tile < total) lines_issue<N>(bufs, g, data, tile, tiles_per_item, t, l);
+  if (base + sub < total) lines_issue<N>(bufs, g, data, base + sub, tiles_per_item, t, l);
   cp_async_commit();
   int cur = 0;
-  for (; tile < total; tile += gridDim.x) {
-    const long long nxt = tile + gridDim.x;
+  for (; base < total; base += step) {
+    const long long tile = base + sub, nxt = tile + step;
     if (nxt < total) lines_issue<N>(bufs + (cur ^ 1) * N * LBUF, g, data, nxt, tiles_per_item, t, l);
     cp_async_commit();
     asm volatile("cp.async.wait_group 1;\n" ::: "memory");
     __syncthreads();
     float2* s = bufs + cur * N * LBUF;
-    const int b = (int)(tile / tiles_per_item);
-    const int line = (int)(tile - (long long)b * tiles_per_item) * LINES + l;
+    const bool have = tile < total;
+    const int b = have ? (int)(tile / tiles_per_item) : 0;
+    const int line = have ? (int)(tile - (long long)b * tiles_per_item) * LINES + l : g.nlines;
     const bool ok = line < g.nlines;
     float2 v[N / T];
     stage_read<N, T, R1, LBUF>(s, v, t, l);
@@ -244,7 +247,7 @@ k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
     } else {
       run_stages<N, T, LBUF, false>(Rad{}, v, s, tw, t, l);
     }
-    float2* base = data + b * g.bstride + (ok ? line_base(g, line) : 0);
+    float2* gbase = data + b * g.bstride + (ok ? line_base(g, line) : 0);
     if constexpr (MODE == 2) {
       const int lc = ok ? line : 0;
       const int mx = g.x0 + lc % g.nxa, my = lc / g.nxa;
@@ -253,14 +256,24 @@ k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
 #pragma unroll
         for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), b);
       run_stages<N, T, LBUF, true>(Rev{}, v, s, tw + N, t, l);
-      lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
+      lines_store<N, RadInfo<Rev>::last>(v, gbase, g.pstride, ok, t);
     } else {
-      lines_store<N, RS>(v, base, g.pstride, ok, t);
+      lines_store<N, RS>(v, gbase, g.pstride, ok, t);
     }
-    __syncthreads();  // the exchanges in s are done before s receives tile + 2 gridDim
+    __syncthreads();  // the exchanges in s are done before s receives the round after next
     cur ^= 1;
   }
   cp_async_wait_all();
+}
+
+template <int N, int MODE, class Op>
+__global__ void __launch_bounds__(threads_for<N>(), min_blocks<N>())
+k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ twg, Op op, int batch) {
+  extern __shared__ float2 smem[];
+  float4* tw = reinterpret_cast<float4*>(smem);  // line fwd [| line rev] tables
+  constexpr int NTAB = MODE == 2 ? 2 : 1;
+  load_twiddles(tw, twg + TW_LINE_FWD * N, NTAB * N);  // visible after the first round's barrier
+  lfft_pipe_run<N, MODE, Op>(data, g, tw, op, batch, smem + 2 * NTAB * N, threadIdx.x, blockIdx.x, gridDim.x, 0);
 }
 
 struct NoOp {
