@@ -69,8 +69,9 @@ def ncu_traffic(pass_name, n, workload, sched):
         return None, "no capture file"
     with open(TRAFFIC_FILE) as f:
         cap = json.load(f)
-    impl = {"kick_xfft_fwd": "x_kick", "kick_final": "x_kick", "psi_z_drift": "psi_z", "psi_x_inv_rho": "x_rho_b",
-            "rho_y_fwd": "h_y", "rho_z_poisson": "h_z", "phi_y_inv": "h_y"}.get(pass_name)
+    impl = {"kick_xfft_fwd": "x_kick", "kick_final": "x_kick", "psi_y_fwd": "psi_y", "psi_z_drift": "psi_z",
+            "psi_y_inv": "psi_y", "psi_x_inv_rho": "x_rho_b", "rho_y_fwd": "h_y", "rho_z_poisson": "h_z",
+            "phi_y_inv": "h_y"}.get(pass_name)
     if impl is None or impl not in sched:
         return None, "pass not captured"
     v = cap["passes"].get(f"{pass_name}/{sched[impl]['impl']}")
