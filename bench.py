@@ -483,7 +483,8 @@ def run_ensemble(args, rank, world, counts=None):
         "passes": {k: {"launches": v["launches"], "ms": round(v["ms"], 4)} for k, v in prof.items()},
         "schedule": {"chosen": sched, "ms_two_steps": sched_ms,
                      "what": "graph: the members' pass launches in one captured graph; persistent: one cooperative "
-                             "kernel for every pass, member and step of a call"},
+                             "kernel for every pass, member and step of a call; streams: the pass launches of each "
+                             "member on its own stream inside the graph"},
         "gpu_launches": int(launches), "launches_per_step": round(launches / K, 3), "e2e": e2e, "clocks": clk,
     }
 

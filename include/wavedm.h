@@ -159,17 +159,21 @@ wdm_status wdm_group_step(wdm_group* g, int32_t nsteps, const double* dts, int32
 /* the same, returning once the graph is enqueued on the group's stream (check
  * the members with wdm_check_finite after synchronising the stream) */
 wdm_status wdm_group_step_async(wdm_group* g, int32_t nsteps, const double* dts, int32_t mode);
-/* How the group runs a call, chosen on its first call by timing both on the
- * members' own state (saved and put back):
- *   0  the members' pass launches, captured into one CUDA graph;
+/* How the group runs a call, chosen on its first call by timing the
+ * candidates on the members' own state (saved and put back):
+ *   0  the members' pass launches, captured into one CUDA graph, one member
+ *      after another on the group's stream;
  *   1  one persistent cooperative kernel for all passes of all members and
  *      steps, a device-wide barrier between passes (its waits bounded: an
  *      abandoned one is reported as WDM_ERR_CUDA), replayed from a graph.
  *      It covers members with axis lengths 16..128 without baryon particles
- *      and with a tide that is constant during the call.
- * sched: the choice (-1 before the first call); ms[0], ms[1]: the timed
+ *      and with a tide that is constant during the call (timed only then);
+ *   2  the members' pass launches in one graph, each member on a stream of
+ *      its own forked from the group's stream, so that the sizes run
+ *      concurrently.
+ * sched: the choice (-1 before the first call); ms[0..2]: the timed
  * milliseconds of two steps under each (-1 when not timed).  The environment
- * variable WDM_GROUP_SCHEDULE=graph|persistent forces the choice. */
+ * variable WDM_GROUP_SCHEDULE=graph|persistent|streams forces the choice. */
 wdm_status wdm_group_schedule(const wdm_group* g, int32_t* sched, double* ms);
 /* the group's cudaStream_t */
 void* wdm_group_stream(const wdm_group* g);

@@ -155,8 +155,8 @@ def test_ensemble_schedule_choice_keeps_the_state(wdm, monkeypatch):
     with wdm.Ensemble([m[0] for m in mem]) as ens:
         ens.step(steps, [m[3] for m in mem])
         sched, ms = ens.schedule
-    assert sched in ("graph", "persistent")
-    assert ms["graph"] > 0 and ms["persistent"] > 0
+    assert sched in ("graph", "persistent", "streams")
+    assert ms["graph"] > 0 and ms["persistent"] > 0 and ms["streams"] > 0
     auto = [m[0].get_psi() for m in mem]
     for m in mem:
         m[0].close()
@@ -167,3 +167,22 @@ def test_ensemble_schedule_choice_keeps_the_state(wdm, monkeypatch):
     for a, m in zip(auto, mem):
         assert np.array_equal(a, m[0].get_psi())
         m[0].close()
+
+
+def test_ensemble_on_forked_streams_equals_one_stream(wdm, monkeypatch):
+    """Each member on a stream of its own inside the group's graph (the sizes
+    run concurrently) gives the bits of the members stepped one after another."""
+    steps = 3
+    out = {}
+    for sched in ("graph", "streams"):
+        monkeypatch.setenv("WDM_GROUP_SCHEDULE", sched)
+        mem = _members(wdm, ENS_SPECS)
+        with wdm.Ensemble([m[0] for m in mem]) as ens:
+            ens.step(steps, [m[3] for m in mem])
+            ens.step(steps, [m[3] for m in mem])
+            assert ens.schedule[0] == sched
+        out[sched] = [m[0].get_psi() for m in mem]
+        for m in mem:
+            m[0].close()
+    for a, b in zip(out["graph"], out["streams"]):
+        assert np.array_equal(a, b)

@@ -328,12 +328,12 @@ class Ensemble:
 
     @property
     def schedule(self):
-        """("graph" | "persistent" | None, {schedule: timed ms of two steps})."""
+        """("graph" | "persistent" | "streams" | None, {schedule: timed ms of two steps})."""
         sched = C.c_int32(-1)
-        ms = (C.c_double * 2)()
+        ms = (C.c_double * 3)()
         check(self.lib.wdm_group_schedule(self._h, C.byref(sched), C.cast(ms, C.c_void_p)))
-        names = {0: "graph", 1: "persistent"}
-        return names.get(sched.value), {"graph": ms[0], "persistent": ms[1]}
+        names = {0: "graph", 1: "persistent", 2: "streams"}
+        return names.get(sched.value), {"graph": ms[0], "persistent": ms[1], "streams": ms[2]}
 
     def close(self):
         if getattr(self, "_h", None):

@@ -1837,11 +1837,16 @@ struct wdm_group {
   };
   std::vector<Entry> cache;
   int64_t launches = 0;
-  // schedule: GROUP_GRAPH (the members' pass launches in one captured graph)
-  // or GROUP_PERSISTENT (one cooperative launch of k_ensemble per call);
+  // schedule: GROUP_GRAPH (the members' pass launches in one captured graph),
+  // GROUP_PERSISTENT (one cooperative launch of k_ensemble per call) or
+  // GROUP_STREAMS (the pass launches of each member on a stream of its own,
+  // forked from and joined to the group's stream inside the graph);
   // chosen by timing both on the first call (see choose_schedule)
   int sched = -1;
-  double sched_ms[2] = {-1.0, -1.0};
+  double sched_ms[3] = {-1.0, -1.0, -1.0};
+  std::vector<cudaStream_t> fork;     // GROUP_STREAMS: one stream per member
+  std::vector<cudaEvent_t> ev_join;   // and its join event
+  cudaEvent_t ev_fork = nullptr;
   // the persistent kernel's member table on the device, for (dts, mode, versions)
   EnsMember* dmem = nullptr;
   unsigned* dwords = nullptr;
@@ -1851,7 +1856,7 @@ struct wdm_group {
   size_t ens_smem = 0;
   int ens_grid = 0;
 };
-enum { GROUP_GRAPH = 0, GROUP_PERSISTENT = 1 };
+enum { GROUP_GRAPH = 0, GROUP_PERSISTENT = 1, GROUP_STREAMS = 2, GROUP_NSCHED = 3 };
 
 // Everything a captured step sequence must not do inside the capture (table
 // uploads with a host sync, the first potential) is done here, eagerly.
@@ -1895,6 +1900,9 @@ wdm_status wdm_group_destroy(wdm_group* g) {
   for (auto& en : g->cache) cudaGraphExecDestroy(en.exec);
   if (g->dmem) cudaFree(g->dmem);
   if (g->dwords) cudaFree(g->dwords);
+  for (cudaStream_t f : g->fork) cudaStreamDestroy(f);
+  for (cudaEvent_t e : g->ev_join) cudaEventDestroy(e);
+  if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   if (g->st) cudaStreamDestroy(g->st);
   delete g;
   return WDM_OK;
@@ -2003,6 +2011,21 @@ static wdm_status group_launch(wdm_group* g, int32_t nsteps, const std::vector<d
                                const std::vector<long long>& ver, int32_t mode, int sched) {
   const size_t n = g->m.size();
   if (sched == GROUP_PERSISTENT) WDM_TRY(build_members(g, dt, mode, ver));
+  if (sched == GROUP_STREAMS && g->fork.size() < n) {
+    if (!g->ev_fork && cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming) != cudaSuccess)
+      return group_fail(WDM_ERR_CUDA, "wdm_group_step: cudaEventCreate failed");
+    while (g->fork.size() < n) {
+      cudaStream_t f = nullptr;
+      cudaEvent_t ev = nullptr;
+      if (cudaStreamCreateWithFlags(&f, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+        if (f) cudaStreamDestroy(f);
+        return group_fail(WDM_ERR_CUDA, "wdm_group_step: stream or event creation failed");
+      }
+      g->fork.push_back(f);
+      g->ev_join.push_back(ev);
+    }
+  }
   wdm_group::Entry* hit = nullptr;
   for (auto& en : g->cache)
     if (en.nsteps == nsteps && en.mode == mode && en.sched == sched && en.dts == dt && en.versions == ver) hit = &en;
@@ -2035,15 +2058,32 @@ static wdm_status group_launch(wdm_group* g, int32_t nsteps, const std::vector<d
         why = std::string("persistent launch: ") + cudaGetErrorString(e);
       }
     } else {
+      const bool streams = sched == GROUP_STREAMS;
+      if (streams && (e = cudaEventRecord(g->ev_fork, g->st)) != cudaSuccess) {
+        bad = WDM_ERR_CUDA;
+        why = std::string("fork: ") + cudaGetErrorString(e);
+      }
       for (size_t i = 0; i < n && bad == WDM_OK; ++i) {
         wdm_ctx* c = g->m[i];
         cudaStream_t own = c->st;
         const bool prof = c->prof.on;
         const int64_t l0 = c->launch_count;
-        c->st = g->st;
+        c->st = streams ? g->fork[i] : g->st;
         c->prof.on = false;
-        bad = step_impl(c, nsteps, dt[i], 0.0, mode);
-        if (bad != WDM_OK) why = c->err;
+        if (streams && (e = cudaStreamWaitEvent(c->st, g->ev_fork, 0)) != cudaSuccess) {
+          bad = WDM_ERR_CUDA;
+          why = std::string("fork: ") + cudaGetErrorString(e);
+        }
+        if (bad == WDM_OK) {
+          bad = step_impl(c, nsteps, dt[i], 0.0, mode);
+          if (bad != WDM_OK) why = c->err;
+        }
+        if (bad == WDM_OK && streams &&
+            ((e = cudaEventRecord(g->ev_join[i], c->st)) != cudaSuccess ||
+             (e = cudaStreamWaitEvent(g->st, g->ev_join[i], 0)) != cudaSuccess)) {
+          bad = WDM_ERR_CUDA;
+          why = std::string("join: ") + cudaGetErrorString(e);
+        }
         launches += c->launch_count - l0;
         c->launch_count = l0;  // counted when the graph runs
         c->st = own;
@@ -2072,15 +2112,20 @@ static wdm_status group_launch(wdm_group* g, int32_t nsteps, const std::vector<d
   return WDM_OK;
 }
 
-// Time both schedules on the members' own state (saved first and put back
+// Time the schedules on the members' own state (saved first and put back
 // after each timing), two steps each after a warm-up call, and keep the
-// faster (the graph of pass launches within 3%).  WDM_GROUP_SCHEDULE=graph or
-// =persistent forces the choice.
+// fastest (the graph of pass launches unless another is faster by more than
+// 3%).  The persistent kernel is timed only for the groups it covers.
+// WDM_GROUP_SCHEDULE=graph|persistent|streams forces the choice.
 static wdm_status choose_schedule(wdm_group* g, const std::vector<double>& dt, const std::vector<long long>& ver,
                                   int32_t mode) {
   if (const char* env = std::getenv("WDM_GROUP_SCHEDULE")) {
     if (!std::strcmp(env, "graph")) {
       g->sched = GROUP_GRAPH;
+      return WDM_OK;
+    }
+    if (!std::strcmp(env, "streams")) {
+      g->sched = GROUP_STREAMS;
       return WDM_OK;
     }
     if (!std::strcmp(env, "persistent")) {
@@ -2090,10 +2135,7 @@ static wdm_status choose_schedule(wdm_group* g, const std::vector<double>& dt, c
       return WDM_OK;
     }
   }
-  if (!persistent_ok(g)) {
-    g->sched = GROUP_GRAPH;
-    return WDM_OK;
-  }
+  const bool pers = persistent_ok(g);
   const size_t n = g->m.size();
   std::vector<float2*> keep(2 * n, nullptr);
   auto release = [&]() {
@@ -2136,7 +2178,8 @@ static wdm_status choose_schedule(wdm_group* g, const std::vector<double>& dt, c
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   wdm_status st = WDM_OK;
-  for (int sch = 0; sch < 2 && st == WDM_OK; ++sch) {
+  for (int sch = 0; sch < GROUP_NSCHED && st == WDM_OK; ++sch) {
+    if (sch == GROUP_PERSISTENT && !pers) continue;
     st = group_launch(g, 2, dt, ver, mode, sch);  // warm-up (and capture)
     restore();
     if (st != WDM_OK) break;
@@ -2161,7 +2204,12 @@ static wdm_status choose_schedule(wdm_group* g, const std::vector<double>& dt, c
     cudaMemsetAsync(c->flag, 0, 2 * sizeof(int), g->st);
   }
   cudaStreamSynchronize(g->st);
-  g->sched = g->sched_ms[GROUP_PERSISTENT] < 0.97 * g->sched_ms[GROUP_GRAPH] ? GROUP_PERSISTENT : GROUP_GRAPH;
+  int best = GROUP_GRAPH;
+  for (int sch = 1; sch < GROUP_NSCHED; ++sch)
+    if (g->sched_ms[sch] > 0.0 && g->sched_ms[sch] < 0.97 * g->sched_ms[GROUP_GRAPH] &&
+        g->sched_ms[sch] < g->sched_ms[best])
+      best = sch;
+  g->sched = best;
   return WDM_OK;
 }
 
@@ -2191,10 +2239,8 @@ static wdm_status group_enqueue(wdm_group* g, int32_t nsteps, const double* dts,
 wdm_status wdm_group_schedule(const wdm_group* g, int32_t* sched, double* ms) {
   if (!g || !sched) return group_fail(WDM_ERR_INVALID, "wdm_group_schedule: null argument");
   *sched = g->sched;
-  if (ms) {
-    ms[0] = g->sched_ms[0];
-    ms[1] = g->sched_ms[1];
-  }
+  if (ms)
+    for (int k = 0; k < GROUP_NSCHED; ++k) ms[k] = g->sched_ms[k];
   return WDM_OK;
 }
 
