@@ -74,3 +74,48 @@ def test_workload2_256_mass_drift_over_1000_steps(wdm):
         ctx.step(wl["steps"], wl["dt"], t0=0.0)
         drift = ctx.reduce()["mass"] / m0 - 1.0
     assert abs(drift) <= 1e-6, drift
+
+
+def test_workload2_256_matches_fp64_oracle(wdm):
+    """256^3 soliton + 4096-wave halo: 50 Strang steps against the oracle (its full
+    1000 steps take the oracle ~18 min on 16 cores; the mass over the 1000 steps
+    is checked above)."""
+    wl = wdm.ics.workload(2)
+    steps, dt, N, L = 50, wl["dt"], wl["n"], wl["L"]
+    g = spe.Grid((N, N, N), (L, L, L))
+    ref = spe.run(wl["psi0"].astype(np.complex64).astype(np.complex128), g, spe.Physics(poisson_coeff=1.0), dt, steps)
+    with _ctx(wdm, wl, "precise", steps + 1) as ctx:
+        ctx.step(steps, dt)
+        psi = ctx.get_psi()
+    assert spe.rel_l2(psi, ref) <= 1e-5
+    assert spe.rel_l2(np.abs(psi) ** 2, np.abs(ref) ** 2) <= 1e-5
+
+
+def test_workload4_ensemble_halos_match_fp64_oracle_over_500_steps(wdm):
+    """The ensemble of workload 4 stepped as one group for its 500 steps; the first
+    halo of each grid size (64^3, 96^3, 128^3, each with its own tide) against the
+    oracle: psi rel-L2 <= 1e-5 and mass drift <= 1e-6."""
+    members = wdm.ics.ensemble_members()
+    counts = {64: 4, 96: 2, 128: 1}
+    ctxs, firsts = [], []
+    for N in (64, 96, 128):
+        mem = [m for m in members if m[0] == N][: counts[N]]
+        L = mem[0][1]
+        ctx = wdm.SPEContext((N, N, N), (L, L, L), poisson_coeff=1.0, batch=len(mem))
+        ctx.set_psi(np.stack([m[2] for m in mem]).astype(np.complex64))
+        ctx.set_tidal(np.stack([m[3] for m in mem]), per_item=True)
+        ctxs.append(ctx)
+        firsts.append(mem[0])
+    dts = [wdm.ics.dt_for(N, f[1]) for N, f in zip((64, 96, 128), firsts)]
+    with wdm.Ensemble(ctxs) as ens:
+        ens.step(500, dts)
+    for c, f, dt in zip(ctxs, firsts, dts):
+        N, L, psi0, T6 = f
+        got = c.get_psi().reshape(c.batch, N, N, N)[0]
+        g = spe.Grid((N, N, N), (L, L, L))
+        phys = spe.Physics(poisson_coeff=1.0, tidal=lambda t, T6=T6: tuple(T6))
+        ref = spe.run(psi0.astype(np.complex64).astype(np.complex128), g, phys, dt, 500)
+        assert spe.rel_l2(got, ref) <= 1e-5, N
+        m_ref = spe.mass(psi0.astype(np.complex64).astype(np.complex128), g)
+        assert abs(spe.mass(got.astype(np.complex128), g) / m_ref - 1.0) <= 1e-6, N
+        c.close()
