@@ -5,9 +5,10 @@
 // B, each straight from and back to global memory (lane t touches points
 // t + T m, so every access is a coalesced run along x), and transforms the
 // two real rows of the density / potential together as the complex line
-// A + iB.  Exchanges between radix stages go through the group's own padded
-// shared buffer with __syncwarp only: no CTA-wide barrier after the twiddle
-// table is loaded, so warps run independently and hide each other's latency.
+// A + iB.  Exchanges between radix stages go through the group's own shared
+// buffer (padded or swizzled per stage boundary, xaddr) with __syncwarp only:
+// no CTA-wide barrier after the twiddle table is loaded, so warps run
+// independently and hide each other's latency.
 #pragma once
 #include "passes.cuh"
 
@@ -24,30 +25,40 @@
 
 namespace wdm {
 
-// Exchange buffer addressing: point p of a group lives at word base + p +
-// (p >> SH).  The shift SH of each stage boundary is chosen at compile time
-// by simulating the shared-memory banks of that boundary's write pattern (the
+// Exchange buffer addressing: point p of a group lives at word base +
+// xaddr(p, code), with a map chosen per stage boundary at compile time by
+// simulating the shared-memory banks of that boundary's write pattern (the
 // Stockham scatter of radix R at stride NS) and the next stage's read pattern
-// for the 32 lanes of a warp (8-byte words, 16 lanes per wavefront).
+// for the 32 lanes of a warp (8-byte words, 16 lanes per wavefront).  The
+// candidates are a padding p + (p >> s) (code s = 2..6; 30: none) and an XOR
+// swizzle of W bits at bit B by the W bits above them,
+// p ^ (((p >> (B + W)) & (2^W - 1)) << B) (code 100 + 10 W + B), which
+// permutes p within its aligned block of 2^(B + W) words and so needs no room
+// beyond the line.
+__host__ __device__ constexpr int xaddr(int p, int code) {
+  return code < 100 ? p + (p >> code)
+                    : (p ^ (((p >> (code % 10 + (code / 10) % 10)) & ((1 << ((code / 10) % 10)) - 1)) << (code % 10)));
+}
+
+// Largest number of distinct words that share a bank pair among 16 lane
+// addresses (8-byte words: bank pair = word mod 16).
 __host__ __device__ constexpr int xbank_degree16(const int* a) {
-  int worst = 1;
-  for (int x = 0; x < 16; ++x) {
-    int d = 0;
-    for (int y = 0; y < 16; ++y) {
-      if (((a[y] - a[x]) & 15) != 0) continue;
-      bool dup = false;
-      for (int z = 0; z < y; ++z)
-        if (a[z] == a[y]) dup = true;
-      if (!dup) ++d;
-    }
-    if (d > worst) worst = d;
+  int cnt[16] = {};
+  for (int y = 0; y < 16; ++y) {
+    bool first = true;
+    for (int z = 0; z < y; ++z)
+      if (a[z] == a[y]) first = false;
+    if (first) ++cnt[a[y] & 15];
   }
+  int worst = 1;
+  for (int b = 0; b < 16; ++b)
+    if (cnt[b] > worst) worst = cnt[b];
   return worst;
 }
 
 template <int N, int T, int NP>
 struct XPad {
-  __host__ __device__ static constexpr int cost(int R, int NS, int RN, int sh) {
+  __host__ __device__ static constexpr int cost(int R, int NS, int RN, int code) {
     int total = 0;
     for (int i = 0; i < N / (R * T); ++i)
       for (int k = 0; k < R; ++k)
@@ -56,7 +67,7 @@ struct XPad {
           for (int q = 0; q < 16; ++q) {
             const int lane = half * 16 + q, g = lane / T, t = lane % T, j = t + T * i;
             const int p = (j / NS) * NS * R + (j % NS) + k * NS;
-            a[q] = g * NP + p + (p >> sh);
+            a[q] = g * NP + xaddr(p, code);
           }
           total += xbank_degree16(a);
         }
@@ -67,15 +78,27 @@ struct XPad {
           for (int q = 0; q < 16; ++q) {
             const int lane = half * 16 + q, g = lane / T, t = lane % T, j = t + T * i;
             const int p = j + k * (N / RN);
-            a[q] = g * NP + p + (p >> sh);
+            a[q] = g * NP + xaddr(p, code);
           }
           total += xbank_degree16(a);
         }
     return total;
   }
+  // the cheapest map; on a tie the one needing the least room (no padding,
+  // then a swizzle, then the smallest padding)
   __host__ __device__ static constexpr int best(int R, int NS, int RN) {
-    int bs = 30, bc = cost(R, NS, RN, 30);  // shift 30: no padding
-    for (int sh = 2; sh <= 6; ++sh) {
+    int bs = 30, bc = cost(R, NS, RN, 30);
+    for (int w = 2; w <= 3; ++w)
+      for (int b = 0; b <= 3; ++b) {
+        if (N % (1 << (b + w)) != 0) continue;
+        const int code = 100 + 10 * w + b;
+        const int c = cost(R, NS, RN, code);
+        if (c < bc) {
+          bc = c;
+          bs = code;
+        }
+      }
+    for (int sh = 6; sh >= 2; --sh) {
       const int c = cost(R, NS, RN, sh);
       if (c < bc) {
         bc = c;
@@ -86,7 +109,31 @@ struct XPad {
   }
 };
 
-template <int N, int T, int R, int NS, int SH>
+// The map of one stage boundary, evaluated once per boundary.
+template <int N, int T, int NP, int R, int NS, int RN>
+struct XMap {
+  static constexpr int code = XPad<N, T, NP>::best(R, NS, RN);
+};
+
+// Words one group's exchange buffer needs for the maps of the stage
+// boundaries from stride NS on (NP0: the row pitch the maps were chosen with).
+template <int N, int T, int NP0, int NS, int R, int... Rest>
+__host__ __device__ constexpr int xextent_from() {
+  if constexpr (sizeof...(Rest) == 0) {
+    return N;
+  } else {
+    constexpr int code = XMap<N, T, NP0, R, NS, First<Rest...>::value>::code;
+    constexpr int here = code < 100 ? xaddr(N - 1, code) + 1 : N;
+    constexpr int rest = xextent_from<N, T, NP0, NS * R, Rest...>();
+    return here > rest ? here : rest;
+  }
+}
+template <int N, int T, int NP0, int... Rs>
+__host__ __device__ constexpr int xextent(Radices<Rs...>) {
+  return xextent_from<N, T, NP0, 1, Rs...>();
+}
+
+template <int N, int T, int R, int NS, int CODE>
 __device__ __forceinline__ void wstage_write(float2* b, const float2* v, int t) {
   constexpr int NB = N / (R * T);
 #pragma unroll
@@ -94,24 +141,18 @@ __device__ __forceinline__ void wstage_write(float2* b, const float2* v, int t) 
     const int j = t + T * i;
     const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const int p = base + k * NS;
-      b[p + (p >> SH)] = v[i * R + k];
-    }
+    for (int k = 0; k < R; ++k) b[xaddr(base + k * NS, CODE)] = v[i * R + k];
   }
 }
 
-template <int N, int T, int R, int SH>
+template <int N, int T, int R, int CODE>
 __device__ __forceinline__ void wstage_read(const float2* b, float2* v, int t) {
   constexpr int NB = N / (R * T);
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     const int j = t + T * i;
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const int p = j + k * (N / R);
-      v[i * R + k] = b[p + (p >> SH)];
-    }
+    for (int k = 0; k < R; ++k) v[i * R + k] = b[xaddr(j + k * (N / R), CODE)];
   }
 }
 
@@ -120,11 +161,11 @@ __device__ __forceinline__ void run_wstages_impl(float2* v, float2* b, const flo
   stage_compute<N, T, R, NS, INV, OFF>(v, tw, t);
   if constexpr (sizeof...(Rest) > 0) {
     constexpr int RN = First<Rest...>::value;
-    constexpr int SH = XPad<N, T, NP>::best(R, NS, RN);
+    constexpr int CODE = XMap<N, T, NP, R, NS, RN>::code;
     __syncwarp();
-    wstage_write<N, T, R, NS, SH>(b, v, t);
+    wstage_write<N, T, R, NS, CODE>(b, v, t);
     __syncwarp();
-    wstage_read<N, T, RN, SH>(b, v, t);
+    wstage_read<N, T, RN, CODE>(b, v, t);
     run_wstages_impl<N, T, NP, INV, NS * R, OFF + NS * (R - 1), Rest...>(v, b, tw, t);
   }
 }
@@ -145,13 +186,13 @@ __device__ __forceinline__ void run_wstages2_impl(float2* va, float2* vb, float2
   stage_compute2<N, T, R, NS, INV, OFF>(va, vb, tw, t);
   if constexpr (sizeof...(Rest) > 0) {
     constexpr int RN = First<Rest...>::value;
-    constexpr int SH = XPad<N, T, NP>::best(R, NS, RN);
+    constexpr int CODE = XMap<N, T, NP, R, NS, RN>::code;
     __syncwarp();
-    wstage_write<N, T, R, NS, SH>(ba, va, t);
-    wstage_write<N, T, R, NS, SH>(bb, vb, t);
+    wstage_write<N, T, R, NS, CODE>(ba, va, t);
+    wstage_write<N, T, R, NS, CODE>(bb, vb, t);
     __syncwarp();
-    wstage_read<N, T, RN, SH>(ba, va, t);
-    wstage_read<N, T, RN, SH>(bb, vb, t);
+    wstage_read<N, T, RN, CODE>(ba, va, t);
+    wstage_read<N, T, RN, CODE>(bb, vb, t);
     run_wstages2_impl<N, T, NP, INV, NS * R, OFF + NS * (R - 1), Rest...>(va, vb, ba, bb, tw, t);
   }
 }
@@ -215,7 +256,11 @@ struct XCfg {
   static constexpr int GROUPS = 32 / T;                // row pairs per warp
   static constexpr int WARPS = 4;                      // warps per CTA
   static constexpr int NT = 32 * WARPS;
-  static constexpr int NP = N + N / 4 + 1;             // padded exchange buffer per group
+  // exchange buffer per group: with one group per warp only the maps' room
+  // (xextent); with several, a pitch of N + N/4 + 1 (odd), which the maps
+  // were chosen for
+  static constexpr int NP0 = N + N / 4 + 1;
+  static constexpr int NP = GROUPS == 1 ? xextent<N, T, NP0>(typename XPlan<N>::Fwd{}) : NP0;
 #if defined(WDM_XTW_GLOBAL)
   static constexpr size_t TW_BYTES = 0;  // twiddles read from global memory (L1), not staged
 #else
