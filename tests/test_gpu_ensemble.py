@@ -91,7 +91,14 @@ def test_ensemble_of_three_sizes(wdm):
         members[k].close()
 
 
-def _members(wdm, specs, centering=None):
+# Baryon particles of one member, 1.5 length units (9 cells) apart along x, so
+# that no two CIC stencils share a cell and the FP32 atomic deposit is the
+# same in every run.
+PARTS_POS = np.array([[-3.0 + 1.5 * p, 0.1 * p, 0.05] for p in range(4)])
+PARTS_MASS = np.array([0.5, 0.3, 0.4, 0.2])
+
+
+def _members(wdm, specs, centering=None, particles_for=None):
     out = []
     for k, (n, batch, L) in enumerate(specs):
         nx, ny, nz = n if isinstance(n, tuple) else (n, n, n)
@@ -109,6 +116,8 @@ def _members(wdm, specs, centering=None):
         ctx.set_tidal(T, per_item=True)
         if centering and k == 0:
             ctx.set_tidal_centering(centering)
+        if particles_for == k:
+            ctx.set_particles(PARTS_POS, PARTS_MASS)
         out.append((ctx, psis, T, (L / nx) ** 2 / 6))
     return out
 
@@ -121,11 +130,12 @@ def test_persistent_ensemble_equals_its_pass_launches(wdm, monkeypatch, mode):
     """One cooperative launch per call (all passes, members and steps) gives the
     bits of the same passes launched one by one with the register-tile line
     passes and the direct x passes, including a tide anchored at the density
-    maximum (its words zeroed and refilled inside the launch)."""
+    maximum (its words zeroed and refilled inside the launch) and a member with
+    baryon particles (their deposit made once, before the launch)."""
     monkeypatch.setenv("WDM_GROUP_SCHEDULE", "persistent")
     monkeypatch.setenv("WDM_SCHEDULE", "tile,tile,tile,tile,direct,direct,direct")
     steps = 4
-    mem = _members(wdm, ENS_SPECS, centering="density_max")
+    mem = _members(wdm, ENS_SPECS, centering="density_max", particles_for=2)
     with wdm.Ensemble([m[0] for m in mem]) as ens:
         l0 = ens.launch_count
         ens.step(steps, [m[3] for m in mem], mode=mode)
@@ -141,6 +151,8 @@ def test_persistent_ensemble_equals_its_pass_launches(wdm, monkeypatch, mode):
             solo.set_tidal(T, per_item=True)
             if k == 0:
                 solo.set_tidal_centering("density_max")
+            if k == 2:
+                solo.set_particles(PARTS_POS, PARTS_MASS)
             solo.step(steps, dt, mode=mode)
             solo.step(steps, dt, mode=mode)
             assert np.array_equal(got, solo.get_psi()), k

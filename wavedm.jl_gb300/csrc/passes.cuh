@@ -490,11 +490,6 @@ struct RhoArgs {
   // ny*nz flags of the rows of rho_b that hold mass (null: every row); the
   // other rows are zero and are not read
   const int* rb_rows = nullptr;
-  // Non-null: the same baryon grid and flags, to be left zero once read (the
-  // rows each row pair used, and their flags), so the next CIC deposit starts
-  // from zero without a clearing kernel.
-  float* rb_zero = nullptr;
-  int* rb_rows_zero = nullptr;
   int write_psi;     // 0: density only (psi is already in real space, left untouched)
   int* nonfinite;    // set to 1 when any density value is NaN/Inf (null: unchecked)
   int* err = nullptr;  // error word of abandoned waits of the staged pass (may be null)

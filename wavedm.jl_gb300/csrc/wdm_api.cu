@@ -168,11 +168,11 @@ struct wdm_ctx {
   std::vector<float2*> slot2_psi, slot2_H;              // segment states, set 1
   cudaStream_t st_rec = nullptr;    // adjoint: recompute of the next segment, beside the reverse sweep
   cudaEvent_t ev_ck = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_bwd[2] = {nullptr, nullptr};
-  // baryons: the next density pass's deposit is already in rho_b (made beside
-  // the potential passes of the previous one, on st_cic)
+  // baryons: the CIC deposit of the current particles is in rho_b.  The
+  // particles are static (src/simulation_main.jl:248-261 computes their
+  // potential once, before the loop), so the deposit is made once per
+  // particle set and every density pass reads it.
   int rb_ready = 0;
-  cudaStream_t st_cic = nullptr;
-  cudaEvent_t ev_p5 = nullptr, ev_dep = nullptr;
   // diagnostics: radii histogram and minimum words (allocated on first use)
   double* diag_wsum = nullptr;
   unsigned long long* diag_wmin = nullptr;
@@ -477,10 +477,8 @@ static LineGeom lines_z(const wdm_ctx* c, int xext, long long pitch, long long b
 // pipeline pieces
 // --------------------------------------------------------------------------
 // density (+baryons) of psi -> H, then the Poisson solve on H (P5..P8).
-// write_psi != 0: psi holds x-spectral data (after P4); the pass inverts it
-// first (with the absorbing mask) and writes real-space psi back.
-// The CIC deposit the next density pass reads, made now on the context stream
-// if none is waiting in rho_b.
+// The CIC deposit of the current particles into rho_b (zero before it), made
+// once per particle set.
 static wdm_status ensure_deposit(wdm_ctx* c) {
   if (c->nparts == 0 || c->rb_ready) return WDM_OK;
   cudaError_t e = run_pass(c, P_CIC_DEPOSIT, [&] {
@@ -491,10 +489,10 @@ static wdm_status ensure_deposit(wdm_ctx* c) {
   return WDM_OK;
 }
 
-// Density pass (P5) and Poisson solve (P6-P8).  With baryons, P5 reads the
-// waiting deposit and leaves rho_b zero; the deposit for the next density pass
-// then runs on st_cic beside P6-P8 (the particles are static, and nothing in
-// between reads rho_b), and the context stream waits for it after P8.
+// Density pass (P5) and Poisson solve (P6-P8).  write_psi != 0: psi holds
+// x-spectral data (after P4); the pass inverts it first (with the absorbing
+// mask) and writes real-space psi back.  With baryons, P5 adds the kept
+// deposit (only the rows it flags are read).
 static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   const int B = c->d.batch;
   if (c->nparts > 0) WDM_TRY(ensure_deposit(c));
@@ -506,9 +504,6 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   ra.mz = mask ? c->mz : nullptr;
   ra.rho_b = c->nparts > 0 ? c->rho_b : nullptr;
   ra.rb_rows = c->nparts > 0 ? c->rb_rows : nullptr;
-  // the density pass leaves the deposit zero behind it (no clearing kernel)
-  ra.rb_zero = c->nparts > 0 ? c->rho_b : nullptr;
-  ra.rb_rows_zero = c->nparts > 0 ? c->rb_rows : nullptr;
   ra.rb_bstride = 0;
   ra.write_psi = write_psi;
   ra.nonfinite = c->flag;
@@ -523,17 +518,6 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
                             c->twx, ra, B, c->st);
   });
   if (e != cudaSuccess) return cuda_fail(c, e, "x_inv_rho");
-  if (c->nparts > 0) {
-    c->rb_ready = 0;
-    WDM_CU(c, cudaEventRecord(c->ev_p5, c->st));
-    WDM_CU(c, cudaStreamWaitEvent(c->st_cic, c->ev_p5, 0));
-    cudaStream_t keep = c->st;
-    c->st = c->st_cic;
-    wdm_status s = ensure_deposit(c);
-    c->st = keep;
-    WDM_TRY(s);
-    WDM_CU(c, cudaEventRecord(c->ev_dep, c->st_cic));
-  }
   if ((e = run_pass(c, P_H_Y_FWD, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, false, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y fwd");
@@ -549,7 +533,6 @@ static wdm_status density_poisson(wdm_ctx* c, int write_psi, double dt_mask) {
   if ((e = run_pass(c, P_H_Y_INV, [&] { return c->ky->lfft(c->H, lines_y(c, c->nxh, c->hpitch, c->nhalf), c->twy, true, B, c->st); })) !=
       cudaSuccess)
     return cuda_fail(c, e, "H y inv");
-  if (c->nparts > 0) WDM_CU(c, cudaStreamWaitEvent(c->st, c->ev_dep, 0));
   c->phi_valid = 1;
   return WDM_OK;
 }
@@ -740,7 +723,6 @@ wdm_status wdm_destroy(wdm_ctx* c) {
   if (c->self_group) wdm_group_destroy(c->self_group);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->st_rec) cudaStreamSynchronize(c->st_rec);
-  if (c->st_cic) cudaStreamSynchronize(c->st_cic);
   void* bufs[] = {c->psi, c->H,  c->twx, c->twy, c->twz, c->kx2, c->ky2,       c->kz2,       c->cxy,
                   c->cz,  c->mx, c->my,  c->mz,  c->V,   c->rho_b, c->rb_rows, c->parts, c->T6b, c->flag, c->scratch_f,
                   c->scratch_h, c->red, c->sums, c->shift, c->shift_in};
@@ -753,9 +735,6 @@ wdm_status wdm_destroy(wdm_ctx* c) {
     for (float2* p : *v)
       if (p) cudaFree(p);
   if (c->st_rec) cudaStreamDestroy(c->st_rec);
-  if (c->st_cic) cudaStreamDestroy(c->st_cic);
-  for (cudaEvent_t e : {c->ev_p5, c->ev_dep})
-    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : {c->ev_ck, c->ev_rec[0], c->ev_rec[1], c->ev_bwd[0], c->ev_bwd[1]})
     if (e) cudaEventDestroy(e);
   for (auto& r : c->prof.pending) {
@@ -1112,7 +1091,7 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
   if (c->parts) cudaFree(c->parts);
   c->parts = nullptr;
   c->nparts = 0;
-  if (c->rb_ready) {  // a deposit of the old particles is waiting: clear it
+  if (c->rb_ready) {  // clear the deposit of the old particles
     WDM_CU(c, cudaMemsetAsync(c->rho_b, 0, sizeof(float) * c->ncell, c->st));
     WDM_CU(c, cudaMemsetAsync(c->rb_rows, 0, sizeof(int) * c->d.ny * c->d.nz, c->st));
     c->rb_ready = 0;
@@ -1127,9 +1106,6 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
     WDM_TRY(dalloc(c, &c->rb_rows, (size_t)c->d.ny * c->d.nz));
     WDM_CU(c, cudaMemsetAsync(c->rb_rows, 0, sizeof(int) * c->d.ny * c->d.nz, c->st));
   }
-  if (!c->st_cic) WDM_CU(c, cudaStreamCreateWithFlags(&c->st_cic, cudaStreamNonBlocking));
-  for (cudaEvent_t* e : {&c->ev_p5, &c->ev_dep})
-    if (!*e) WDM_CU(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   // cell index and fractions in FP64 on the host (particles are static)
   std::vector<CicParticle> h((size_t)n);
   const double d[3] = {c->dx, c->dy, c->dz};
@@ -1865,8 +1841,8 @@ static wdm_status prepare_capture(wdm_ctx* c, double dt) {
   if (c->d.phase_mode == WDM_PHASE_PRECISE) WDM_TRY(ensure_drift_tables(c, dt));
   if (c->d.absorb_alpha != 0.0) WDM_TRY(ensure_mask_tables(c, dt));
   if (!c->phi_valid) WDM_TRY(density_poisson(c, 0, dt));
-  // a captured sequence assumes a deposit is waiting when it starts (each
-  // density pass leaves the next one), so a replay never deposits twice
+  // the deposit is made once per particle set, here, so a captured sequence
+  // holds none
   WDM_TRY(ensure_deposit(c));
   WDM_CU(c, cudaStreamSynchronize(c->st));
   return WDM_OK;
@@ -1915,7 +1891,6 @@ int64_t wdm_group_launch_count(const wdm_group* g) { return g ? g->launches : 0;
 static bool persistent_ok(const wdm_group* g) {
   for (const wdm_ctx* c : g->m) {
     if (!ens_size_supported(c->d.nx) || !ens_size_supported(c->d.ny) || !ens_size_supported(c->d.nz)) return false;
-    if (c->nparts > 0) return false;
     if (c->tide_on == 1 && c->tide.size() > 6) return false;
   }
   return true;
@@ -1957,6 +1932,8 @@ static wdm_status build_members(wdm_group* g, const std::vector<double>& dt, int
     ra.mx = mask ? c->mx : nullptr;
     ra.my = mask ? c->my : nullptr;
     ra.mz = mask ? c->mz : nullptr;
+    ra.rho_b = c->nparts > 0 ? c->rho_b : nullptr;  // the kept deposit (prepare_capture made it)
+    ra.rb_rows = c->nparts > 0 ? c->rb_rows : nullptr;
     ra.write_psi = 1;
     ra.nonfinite = c->flag;
     ra.shift = c->shift;

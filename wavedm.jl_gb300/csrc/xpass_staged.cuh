@@ -349,7 +349,6 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
     }
     }
     if constexpr (CEN) centre_pair_done<N>(a, rg, ca, cs, b, ra, true, t);
-    if (a.rb_zero) clear_rb_pair<N>(a, rg, b, ra, true, t, (mcur >> (2 * g)) & 3u);
     mcur = mnext;
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);

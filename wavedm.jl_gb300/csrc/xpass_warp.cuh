@@ -517,35 +517,6 @@ __device__ __forceinline__ void centre_pair_done(const RhoArgs& a, const RowGeom
   }
 }
 
-// After both rows of a pair used their baryon density: zero the flagged rows
-// at the positions this lane read (each lane clears what it read, so no lane
-// races another) and reset the rows' flags.  All lanes of the warp call it;
-// ok selects the lane groups that hold a pair.  flags: bit h set when row
-// ra + h is flagged (both bits without flags).
-template <int N>
-__device__ __forceinline__ void clear_rb_pair(const RhoArgs& a, const RowGeom& rg, int b, int ra, bool ok, int t,
-                                              unsigned flags) {
-  constexpr int T = XCfg<N>::T;
-  constexpr int RS = RadInfo<typename XPlan<N>::Fwd>::last;
-  __syncwarp();
-  if (ok)
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int r = ra + half;
-      if (!((flags >> half) & 1u)) continue;
-      float* row = a.rb_zero + b * a.rb_bstride + (long long)r * rg.pitch;
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) row[slot_pos<N, T, RS>(t, i, k)] = 0.f;
-    }
-  __syncwarp();  // every lane has read the flags before they are reset
-  if (ok && t == 0 && a.rb_rows_zero) {
-    a.rb_rows_zero[ra] = 0;
-    a.rb_rows_zero[ra + 1] = 0;
-  }
-}
-
 // The slice of an x pass one warp runs: warp units u0, u0 + ustride, ...,
 // with the twiddle tables of the pass (x fwd | x rev) in shared memory at tw
 // and this lane group's exchange buffer (XCfg<N>::NP entries) at buf.
@@ -707,10 +678,6 @@ __device__ __forceinline__ void xw_inv_rho_units(float2* __restrict__ psi, float
       inv_rho_row<N, CEN>(v, a, rg, r, ok, row, rb, shift, half, rho0, z, buf, tw, t, ca);
     }
     if constexpr (CEN) centre_pair_done<N>(a, rg, ca, cs, b, ra, ok, t);
-    if (a.rb_zero) {
-      const unsigned fl = ok ? (!a.rb_rows ? 3u : (a.rb_rows[ra] ? 1u : 0u) | (a.rb_rows[ra + 1] ? 2u : 0u)) : 0u;
-      clear_rb_pair<N>(a, rg, b, ra, ok, t, fl);
-    }
     reorder<N, T, RS, R1>(z, v);
     run_wstages<N, T, C::NP, false>(Rad{}, v, buf, tw, t);
     float2* hrow = H + b * hbstride + ra * hpitch;
