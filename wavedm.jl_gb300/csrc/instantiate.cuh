@@ -91,6 +91,29 @@ struct Launch {
     return encode_map_c64(map, data, dims, strides, box);
   }
 
+  // Tensor map of the edge tiles of g (the last column when nxa = 16 m + 1,
+  // 8 rows per tile; k_lfft_tma): the lines' axis outermost, a box of 2
+  // columns x 8 rows x BOXP points starting at column nxa - 1, whose x offset
+  // (nxa - 1) * 8 bytes must be a multiple of 16.  false: no edge tiles.
+  static bool edge_map(CUtensorMap* map, const float2* data, const LineGeom& g, int batch) {
+    using TT = TmaTile<N>;
+    if (g.axis != 1 && g.axis != 2) return false;
+    if (g.nxa % LINES != 1 || g.nxa < LINES || (g.nxa - 1) % 2 != 0 || g.rows <= 0 || g.rows % 8 != 0) return false;
+    const uint64_t e = sizeof(float2);
+    uint64_t dims[4] = {(uint64_t)g.nxa, (uint64_t)g.rows, (uint64_t)N, (uint64_t)batch};
+    uint64_t strides[3];
+    if (g.axis == 1) {  // rows (z) at pitch * N, points (y) at pitch
+      strides[0] = (uint64_t)g.pitch * N * e;
+      strides[1] = (uint64_t)g.pitch * e;
+    } else {  // rows (y) at pitch, points (z) at pitch * rows
+      strides[0] = (uint64_t)g.pitch * e;
+      strides[1] = (uint64_t)g.pitch * g.rows * e;
+    }
+    strides[2] = (uint64_t)g.bstride * e;
+    const uint32_t box[4] = {2, 8, (uint32_t)TT::BOXP, 1};
+    return encode_map_c64(map, data, dims, strides, box);
+  }
+
   // persistent line pass: one wave of resident CTAs walking all tiles
   template <int MODE, class Op>
   static cudaError_t lpipe(float2* data, const LineGeom& g, const float4* tw, const Op& op, int batch,
@@ -98,15 +121,22 @@ struct Launch {
     if (g.nlines <= 0 || batch <= 0) return cudaSuccess;
 #if !defined(WDM_LINE_PIPELINE) && !defined(WDM_LINE_TILE)
     {
-      CUtensorMap map;
+      CUtensorMap map, emap;
       if (g.impl == LINE_IMPL_TMA && line_map(&map, data, g, batch)) {
         constexpr size_t SMEM = ltma_smem_bytes<N, MODE>();
         cudaError_t e;
         if ((e = prep_once<k_lfft_tma<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
-        const long long tiles = (long long)g.rows * ((g.nxa + LINES - 1) / LINES) * batch;
+        LineGeom ge = g;
+        ge.edge = 0;
+#ifndef WDM_NO_EDGE_TILES
+        if (edge_map(&emap, data, g, batch)) ge.edge = g.rows / 8;
+#endif
+        if (!ge.edge) emap = map;  // not read
+        const int tx = ge.edge ? g.nxa / LINES : (g.nxa + LINES - 1) / LINES;
+        const long long tiles = ((long long)g.rows * tx + ge.edge) * batch;
         const long long cap = (long long)resident_ctas<k_lfft_tma<N, MODE, Op>>(NT, SMEM) * sm_count();
         const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
-        k_lfft_tma<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, map, g, tw, op, batch);
+        k_lfft_tma<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, map, emap, ge, tw, op, batch);
         ++tl_kernel_launches;
         return cudaGetLastError();
       }

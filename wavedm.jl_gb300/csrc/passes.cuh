@@ -58,6 +58,11 @@ struct LineGeom {
   int* err = nullptr;    // device-visible error word (bounded waits), may be null
   int x0 = 0;            // x column of the first line (k-space operators see mx = x0 + column)
   int impl = 0;          // LINE_IMPL_TMA or LINE_IMPL_TILE (chosen per pass by the autotuner)
+  // TMA pass only: edge tiles per batch item for the last column when
+  // nxa = 16 m + 1 (the kx = N/2 column of a half spectrum), 0: none.  The
+  // rows' full tiles then cover columns 0 .. 16 m - 1, and each edge tile
+  // holds the last column of 8 rows (filled in by the launcher).
+  int edge = 0;
 };
 
 // Implementations of a line pass: the TMA-fed persistent pass (used where the
@@ -366,15 +371,27 @@ __host__ __device__ constexpr size_t ltma_smem_bytes() {
          (MODE == 2 ? sizeof(float) * N : 0);
 }
 
+// Edge tiles: the map `emap` views the array with the lines' axis outermost
+// and a box of 2 columns x 8 rows x BOXP points, so that the box lands as
+// [point][row][column], the [N][LINES] layout of a full tile with line
+// l = 2 row + column.  The box starts at the last column, x = nxa - 1; its
+// second column lies past the tensor, is filled with zeros and never stored.
+// A tile's per-item number: rows * tx full tiles, then g.edge edge tiles.
 template <int N>
-__device__ __forceinline__ void ltma_issue(const CUtensorMap* map, float2* slot, uint64_t* bar, const LineGeom& g,
-                                           long long tile, int tx) {
+__device__ __forceinline__ void ltma_issue(const CUtensorMap* map, const CUtensorMap* emap, float2* slot,
+                                           uint64_t* bar, const LineGeom& g, long long tile, int tx) {
   using TT = TmaTile<N>;
-  const long long per_item = (long long)g.rows * tx;
+  const long long per_item = (long long)g.rows * tx + g.edge;
   const int b = (int)(tile / per_item);
   const int rem = (int)(tile - (long long)b * per_item);
-  const int row = rem / tx, x0 = (rem - row * tx) * LINES;
   mbar_expect_tx(bar, TT::BYTES);
+  if (rem >= g.rows * tx) {
+    const int e = rem - g.rows * tx;
+#pragma unroll
+    for (int q = 0; q < TT::NBOX; ++q) tma_load_4d(slot + q * TT::BOXP * LINES, emap, bar, g.nxa - 1, 8 * e, q * TT::BOXP, b);
+    return;
+  }
+  const int row = rem / tx, x0 = (rem - row * tx) * LINES;
 #pragma unroll
   for (int q = 0; q < TT::NBOX; ++q) {
     if (g.axis == 1)
@@ -391,8 +408,8 @@ __host__ __device__ constexpr int ltma_min_blocks() {
 
 template <int N, int MODE, class Op>
 __global__ void __launch_bounds__(threads_for<N>(), ltma_min_blocks<N>())
-k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, LineGeom g,
-           const float4* __restrict__ twg, Op op, int batch) {
+k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap emap,
+           LineGeom g, const float4* __restrict__ twg, Op op, int batch) {
   using P = Plan<N>;
   using TT = TmaTile<N>;
   constexpr int T = P::T;
@@ -408,9 +425,10 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
   const int tid = threadIdx.x;
   const int l = tid % LINES, t = tid / LINES;
   // tiles of 16 columns; when 16 does not divide nxa the last tile of a row
-  // reaches past the tensor (zero-filled by the copy, not stored)
-  const int tx = (g.nxa + LINES - 1) / LINES;
-  const long long per_item = (long long)g.rows * tx;
+  // reaches past the tensor (zero-filled by the copy, not stored), unless the
+  // last column goes to edge tiles
+  const int tx = g.edge ? g.nxa / LINES : (g.nxa + LINES - 1) / LINES;
+  const long long per_item = (long long)g.rows * tx + g.edge;
   const long long total = per_item * batch;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
@@ -422,14 +440,14 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
     for (int i = tid; i < N; i += blockDim.x) optab[i] = op.table_entry(i);
   __syncthreads();
   long long tile = blockIdx.x;
-  if (tid == 0 && tile < total) ltma_issue<N>(&map, slots, &bar[0], g, tile, tx);
+  if (tid == 0 && tile < total) ltma_issue<N>(&map, &emap, slots, &bar[0], g, tile, tx);
   unsigned pending = tile < total ? 1u : 0u;  // bit s: slot s has a copy in flight
   for (int it = 0; tile < total; tile += gridDim.x, ++it) {
     const int cur = it & 1;
     const unsigned par = (unsigned)(it >> 1) & 1u;  // slot cur's k-th use completes phase k
     const long long nxt = tile + gridDim.x;
     if (nxt < total) {
-      if (tid == 0) ltma_issue<N>(&map, slots + (cur ^ 1) * N * LINES, &bar[cur ^ 1], g, nxt, tx);
+      if (tid == 0) ltma_issue<N>(&map, &emap, slots + (cur ^ 1) * N * LINES, &bar[cur ^ 1], g, nxt, tx);
       pending |= 1u << (cur ^ 1);
     }
     const bool landed = mbar_wait_bounded(&bar[cur], par);
@@ -445,7 +463,9 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, L
     float2* s = slots + cur * N * LINES;
     const int b = (int)(tile / per_item);
     const int rem = (int)(tile - (long long)b * per_item);
-    const int row = rem / tx, x = (rem - row * tx) * LINES + l;
+    const bool edge = rem >= g.rows * tx;
+    const int row = edge ? 8 * (rem - g.rows * tx) + (l >> 1) : rem / tx;
+    const int x = edge ? g.nxa - 1 + (l & 1) : (rem - row * tx) * LINES + l;
     const bool ok = x < g.nxa;
     const int mx = ok ? x : 0;
     float2* base = data + b * g.bstride + (long long)row * g.outer + mx;
