@@ -121,21 +121,29 @@ struct DriftOp {
   float sign;             // +1: exp(-i k^2 dt/2); -1: its conjugate (the drift adjoint)
   int precise;
   static constexpr bool TABLE = false;
-  __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int) const {
-    if (precise) {
+  static constexpr bool FORMS = true;  // the precise / plain choice is made once per line (op_points)
+  // ROT: cz may hold flagged entries (rot != 0)
+  template <bool PRECISE, bool ROT>
+  __device__ __forceinline__ float2 at(float2 v, int mx, int my, int pos) const {
+    if constexpr (PRECISE) {
       const bool conj = sign < 0.f;
       const float4 wz = cz[pos];
       const float4 wxy = cxy[(long long)my * nxy + mx];
-      const float2 u = rot ? twiddle_mul<true>(v, wz, conj) : twiddle_mul<false>(v, wz, conj);
+      const float2 u = twiddle_mul<ROT>(v, wz, conj);
       return twiddle_mul<false>(u, wxy, conj);
     }
     const float th = sign * (kx2[mx] + ky2[my] + kz2[pos]) * half_dt;
     const float2 sc = sincos_plain(th);
     return cmul(v, make_float2(sc.y * scale, -sc.x * scale));
   }
+  __device__ __forceinline__ float2 operator()(float2 v, int mx, int my, int pos, int) const {
+    return precise ? (rot ? at<true, true>(v, mx, my, pos) : at<true, false>(v, mx, my, pos))
+                   : at<false, false>(v, mx, my, pos);
+  }
 };
 
 struct PoissonOp {
+  static constexpr bool FORMS = false;
   const float* kx2;
   const float* ky2;
   const float* kz2;
@@ -156,6 +164,42 @@ struct PoissonOp {
     return make_float2(v.x * f, v.y * f);
   }
 };
+
+// The k-space operator at every point of one line held at radix-RS slots
+// (mode (mx, my, pos) of batch item b): from the table staged in shared memory
+// (TAB, for operators that have one), or with a runtime form tested once for
+// the line's points.
+template <bool A, bool B>
+struct BoolPair {
+  static constexpr bool first = A, second = B;
+};
+
+template <int N, int T, int RS, bool TAB, class Op>
+__device__ __forceinline__ void op_points(const Op& op, float2* v, int mx, int my, int t, int b, const float* tab) {
+  if constexpr (TAB && Op::TABLE) {
+#pragma unroll
+    for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+      for (int k = 0; k < RS; ++k) v[i * RS + k] = op.with_table(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), tab);
+  } else if constexpr (Op::FORMS) {
+    auto line = [&](auto form) {
+      constexpr bool P = decltype(form)::first, R = decltype(form)::second;
+#pragma unroll
+      for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+        for (int k = 0; k < RS; ++k)
+          v[i * RS + k] = op.template at<P, R>(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k));
+    };
+    if (!op.precise) line(BoolPair<false, false>{});
+    else if (op.rot) line(BoolPair<true, true>{});
+    else line(BoolPair<true, false>{});
+  } else {
+#pragma unroll
+    for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), b);
+  }
+}
 
 // ----------------------------------------------------------------------------
 // strided-line passes (y or z axis)
@@ -256,10 +300,7 @@ __device__ __forceinline__ void lfft_pipe_run(float2* __restrict__ data, const L
     if constexpr (MODE == 2) {
       const int lc = ok ? line : 0;
       const int mx = g.x0 + lc % g.nxa, my = lc / g.nxa;
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), b);
+      op_points<N, T, RS, false>(op, v, mx, my, t, b, nullptr);
       run_stages<N, T, LBUF, true>(Rev{}, v, s, tw + N, t, l);
       lines_store<N, RadInfo<Rev>::last>(v, gbase, g.pstride, ok, t);
     } else {
@@ -283,6 +324,7 @@ k_lfft_pipe(float2* __restrict__ data, LineGeom g, const float4* __restrict__ tw
 
 struct NoOp {
   static constexpr bool TABLE = false;
+  static constexpr bool FORMS = false;
   __device__ __forceinline__ float2 operator()(float2 v, int, int, int, int) const { return v; }
 };
 
@@ -315,10 +357,7 @@ __device__ __forceinline__ void lfft_tile_one(float2* __restrict__ data, const L
   if constexpr (MODE == 2) {
     const int lc = ok ? line : 0;
     const int mx = g.x0 + lc % g.nxa, my = lc / g.nxa;
-#pragma unroll
-    for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-      for (int k = 0; k < RS; ++k) v[i * RS + k] = op(v[i * RS + k], mx, my, slot_pos<N, T, RS>(t, i, k), b);
+    op_points<N, T, RS, false>(op, v, mx, my, t, b, nullptr);
     run_stages<N, T, LPITCH, true>(Rev{}, v, s, tw + N, t, l);
     lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
   } else {
@@ -477,15 +516,7 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, c
       run_stages<N, T, LINES, false>(Rad{}, v, s, tw, t, l);
     }
     if constexpr (MODE == 2) {
-#pragma unroll
-      for (int i = 0; i < N / (RS * T); ++i)
-#pragma unroll
-        for (int k = 0; k < RS; ++k) {
-          if constexpr (Op::TABLE)
-            v[i * RS + k] = op.with_table(v[i * RS + k], g.x0 + mx, row, slot_pos<N, T, RS>(t, i, k), optab);
-          else
-            v[i * RS + k] = op(v[i * RS + k], g.x0 + mx, row, slot_pos<N, T, RS>(t, i, k), b);
-        }
+      op_points<N, T, RS, true>(op, v, g.x0 + mx, row, t, b, optab);
       run_stages<N, T, LINES, true>(Rev{}, v, s, tw + N, t, l);
       lines_store<N, RadInfo<Rev>::last>(v, base, g.pstride, ok, t);
     } else {
@@ -601,8 +632,11 @@ __device__ inline void tide_frame_of(float* out, const float* T6, const unsigned
 // kick_factor gives the phase factor once, so that a caller applying the same
 // kick to two states (the adjoint: psi and lam) evaluates it once:
 // exp(-i r) - 1 in the precise form, exp(-i th) in the plain form.
-__device__ __forceinline__ float2 kick_factor(float pot, const KickArgs& a) {
-  if (a.precise) {
+// The _t forms take the form as a compile-time flag, so that a caller can
+// test a.precise once for many points.
+template <bool PRECISE>
+__device__ __forceinline__ float2 kick_factor_t(float pot, const KickArgs& a) {
+  if constexpr (PRECISE) {
     const float th = pot * a.dt_hi;
     const float te = fmaf(pot, a.dt_hi, -th) + pot * a.dt_lo;
     const float n = rintf(th * 0.15915494309189535f);
@@ -613,14 +647,25 @@ __device__ __forceinline__ float2 kick_factor(float pot, const KickArgs& a) {
   return make_float2(sc.y, -sc.x);
 }
 
+__device__ __forceinline__ float2 kick_factor(float pot, const KickArgs& a) {
+  if (a.precise) return kick_factor_t<true>(pot, a);
+  return kick_factor_t<false>(pot, a);
+}
+
 // v exp(-i th), or v exp(+i th) (CONJ), from the factor of kick_factor.  In
 // the precise form the conjugate factor is bit for bit the factor of -pot (the
 // reduction and the series are odd/even in th), so CONJ is a kick by -pot.
+template <bool PRECISE, bool CONJ = false>
+__device__ __forceinline__ float2 kick_by_t(float2 v, float2 e) {
+  if (CONJ) e.y = -e.y;
+  if constexpr (PRECISE) return make_float2(v.x + (v.x * e.x - v.y * e.y), v.y + (v.x * e.y + v.y * e.x));
+  return cmul(v, e);
+}
+
 template <bool CONJ = false>
 __device__ __forceinline__ float2 kick_by(float2 v, float2 e, const KickArgs& a) {
-  if (CONJ) e.y = -e.y;
-  if (a.precise) return make_float2(v.x + (v.x * e.x - v.y * e.y), v.y + (v.x * e.y + v.y * e.x));
-  return cmul(v, e);
+  if (a.precise) return kick_by_t<true, CONJ>(v, e);
+  return kick_by_t<false, CONJ>(v, e);
 }
 
 __device__ __forceinline__ float2 apply_kick(float2 v, float pot, const KickArgs& a) {

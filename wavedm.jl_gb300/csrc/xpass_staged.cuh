@@ -16,13 +16,26 @@
 #pragma once
 #include "xpass_warp.cuh"
 
-// Largest number of resident CTAs per SM the staged kernels are compiled for
-// (registers per thread = 65536 / (128 threads x that number)).  At N = 384
-// the shared memory allows 4, but the kick compiled for 4 (122 registers)
-// issued 6% more instructions and measured 0.353 ms against 0.337 ms for 3
-// CTAs of up to 170 registers.
-#ifndef WDM_XS_MINB_CAP
-#define WDM_XS_MINB_CAP 3
+namespace wdm {
+// Largest number of resident CTAs per SM the staged kernels of size N are
+// compiled for (registers per thread = 65536 / (128 threads x that number));
+// WDM_XS_MINB_CAP overrides it for every size.  At N = 384 the shared memory
+// allows 4, but the kick compiled for 4 (122 registers) issued 6% more
+// instructions and measured 0.353 ms against 0.337 ms for 3 CTAs of up to
+// 170 registers.
+template <int N>
+struct XStageCap {
+  static constexpr int value = 4;
+};
+template <>
+struct XStageCap<384> {
+  static constexpr int value = 3;
+};
+}  // namespace wdm
+#ifdef WDM_XS_MINB_CAP
+#define WDM_XS_CAP(N) WDM_XS_MINB_CAP
+#else
+#define WDM_XS_CAP(N) XStageCap<N>::value
 #endif
 // 1: the staged density pass transforms the two rows of a pair side by side
 #ifndef WDM_XS_PAIR
@@ -46,10 +59,11 @@ struct XStage {
   static constexpr size_t WARP_BYTES = A_BYTES + B_BYTES;
   static constexpr size_t BASE = C::SMEM;  // after the twiddle tables and exchange buffers
   static constexpr size_t SMEM = BASE + C::WARPS * WARP_BYTES + C::WARPS * 2 * sizeof(uint64_t);
-  // resident CTAs per SM the shared memory allows (at most WDM_XS_MINB_CAP),
-  // for the register budget
+  // resident CTAs per SM the shared memory allows (at most XStageCap), for
+  // the register budget
+  static constexpr int CAP = WDM_XS_CAP(N);
   static constexpr int MINB_RAW = (int)((228u * 1024u) / (SMEM + 1024u));
-  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > WDM_XS_MINB_CAP ? WDM_XS_MINB_CAP : MINB_RAW);
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > CAP ? CAP : MINB_RAW);
   static_assert(BASE % 16 == 0 && A_BYTES % 16 == 0 && B_BYTES % 16 == 0, "16-byte aligned slots");
   static_assert(2 * PSI_P >= C::NP, "a pair's psi rows hold one exchange buffer");
 };
@@ -83,7 +97,7 @@ struct XStageAdj : XStage<N> {
   static constexpr size_t WARP_BYTES = B::A_BYTES + 2 * B::B_BYTES;
   static constexpr size_t SMEM = B::BASE + B::C::WARPS * WARP_BYTES + B::C::WARPS * 2 * sizeof(uint64_t);
   static constexpr int MINB_RAW = (int)((228u * 1024u) / (SMEM + 1024u));
-  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > WDM_XS_MINB_CAP ? WDM_XS_MINB_CAP : MINB_RAW);
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > B::CAP ? B::CAP : MINB_RAW);
 };
 
 #define WDM_XSTAGE_PROLOGUE WDM_XSTAGE_PROLOGUE_T(XStage<N>)

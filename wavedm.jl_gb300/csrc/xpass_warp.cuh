@@ -358,7 +358,7 @@ __device__ __forceinline__ void store_packed_half(const float2* v, float2* buf, 
 // of the x plan, where the potential's C2R leaves it), phi its potential at the
 // same slots; v <- v exp(-i dt pot).
 template <int N, int R1 = RadInfo<typename XPlan<N>::Fwd>::last>
-__device__ __forceinline__ void kick_points(float2* v, const float* phi, const float* T6, const KickArgs& a,
+__device__ __forceinline__ void kick_points(float2* v, float* phi, const float* T6, const KickArgs& a,
                                             const RowGeom& rg, int r, int b, bool ok, int t) {
   using C = XCfg<N>;
   constexpr int T = C::T;
@@ -369,21 +369,40 @@ __device__ __forceinline__ void kick_points(float2* v, const float* phi, const f
   // 1/2 x^T T x = 1/2 Txx x^2 + Txy x y + Txz x z + (1/2 Tyy y^2 + Tyz y z + 1/2 Tzz z^2) + C
   const float cyz = 0.5f * T6[1] * fy * fy + T6[5] * fy * fz + 0.5f * T6[2] * fz * fz + T6[9];
   const float lin = T6[3] * fy + T6[4] * fz;
+  // The potential is completed in phi (which the caller gives up), each
+  // optional term tested once for the row's points and added in the same
+  // order at every point; the phase form is chosen once as well, so that the
+  // loop of the precise form holds no call of the plain form's out-of-line
+  // sincos.  Per-point tests had kept the compiler from interleaving the
+  // points' arithmetic: this took the kick from 276 M to 244 M warp
+  // instructions and from 0.337 to 0.288 ms at 384^3.
+  constexpr int NQ = N / T;
+  if (a.tidal) {
 #pragma unroll
-  for (int i = 0; i < N / (R1 * T); ++i)
+    for (int i = 0; i < N / (R1 * T); ++i)
 #pragma unroll
-    for (int k = 0; k < R1; ++k) {
-      const int q = i * R1 + k;
-      const int x = slot_pos<N, T, R1>(t, i, k);
-      float pot = phi[q];
-      if (a.tidal) {
-        const float fx = T6[6] + a.dx * x;
-        pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
+      for (int k = 0; k < R1; ++k) {
+        const float fx = T6[6] + a.dx * slot_pos<N, T, R1>(t, i, k);
+        phi[i * R1 + k] += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
       }
-      if (a.kerr != 0.f) pot += a.kerr * (v[q].x * v[q].x + v[q].y * v[q].y);
-      if (vrow && ok) pot += vrow[x];
-      v[q] = apply_kick(v[q], pot, a);
-    }
+  }
+  if (a.kerr != 0.f) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) phi[q] = fmaf(a.kerr, fmaf(v[q].x, v[q].x, v[q].y * v[q].y), phi[q]);
+  }
+  if (vrow && ok) {
+#pragma unroll
+    for (int i = 0; i < N / (R1 * T); ++i)
+#pragma unroll
+      for (int k = 0; k < R1; ++k) phi[i * R1 + k] += vrow[slot_pos<N, T, R1>(t, i, k)];
+  }
+  if (a.precise) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = kick_by_t<true>(v[q], kick_factor_t<true>(phi[q], a));
+  } else {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = kick_by_t<false>(v[q], kick_factor_t<false>(phi[q], a));
+  }
 }
 
 // Store a row held at radix-R slots (when ok).
@@ -402,7 +421,7 @@ __device__ __forceinline__ void store_row(float2* row, const float2* v, bool ok,
 // first stage wants radix-R1 slots (a renaming of the same registers), and
 // store to `row` (when ok).
 template <int N, bool FWD>
-__device__ __forceinline__ void kick_row(float2* v, const float* phi, const float* T6, const KickArgs& a,
+__device__ __forceinline__ void kick_row(float2* v, float* phi, const float* T6, const KickArgs& a,
                                          const RowGeom& rg, int r, int b, bool ok, float2* row, float2* buf,
                                          const float4* tw, int t) {
   using C = XCfg<N>;
@@ -604,21 +623,38 @@ __device__ __forceinline__ void rho_row_post(float2* v, const RhoArgs& a, const 
     }
     store_row<N, RS>(row, v, ok, t);
   }
+  // The density is formed in place (rho0 for row A, the y parts of z for
+  // row B), each optional step tested once for the row's points.
+  constexpr int NQ = N / T;
+  auto d = [&](int q) -> float& { return half == 0 ? rho0[q] : z[q].y; };
 #pragma unroll
-  for (int i = 0; i < N / (RS * T); ++i)
+  for (int q = 0; q < NQ; ++q) {
+    if (half != 0) z[q].x = rho0[q];
+    d(q) = fmaf(v[q].x, v[q].x, v[q].y * v[q].y);
+  }
+  if (ok && a.nonfinite) {
+    bool bad = false;
 #pragma unroll
-    for (int k = 0; k < RS; ++k) {
-      const float2 q = v[i * RS + k];
-      float d = q.x * q.x + q.y * q.y;
-      if (ok && a.nonfinite && !isfinite(d)) *a.nonfinite = 1;
-      if constexpr (CEN) {
+    for (int q = 0; q < NQ; ++q) bad |= !isfinite(d(q));
+    if (bad) *a.nonfinite = 1;
+  }
+  if constexpr (CEN) {
+#pragma unroll
+    for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+      for (int k = 0; k < RS; ++k) {
         const int x = slot_pos<N, T, RS>(t, i, k);
-        ca.add(d, (unsigned)r * (unsigned)N + (unsigned)x, x, half);
+        ca.add(d(i * RS + k), (unsigned)r * (unsigned)N + (unsigned)x, x, half);
       }
-      if (rb && ok) d += rb[slot_pos<N, T, RS>(t, i, k)];
-      if (half == 0) rho0[i * RS + k] = d - shift;
-      else z[i * RS + k] = make_float2(rho0[i * RS + k], d - shift);
-    }
+  }
+  if (rb && ok) {
+#pragma unroll
+    for (int i = 0; i < N / (RS * T); ++i)
+#pragma unroll
+      for (int k = 0; k < RS; ++k) d(i * RS + k) += rb[slot_pos<N, T, RS>(t, i, k)];
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) d(q) -= shift;
 }
 
 // One row of P5: v holds psi row r (write_psi: x-spectral at radix-R1 slots,
@@ -832,7 +868,7 @@ __device__ __forceinline__ void adj_kick_points(const float2* v, const float* ph
       const float fx = a.x0 + a.dx * x;
       float pot = phi[q];
       if (a.tidal) pot += fmaf(fx, fmaf(0.5f * T6[0], fx, lin), cyz);
-      if (a.kerr != 0.f) pot += a.kerr * (pre.x * pre.x + pre.y * pre.y);
+      if (a.kerr != 0.f) pot = fmaf(a.kerr, fmaf(pre.x, pre.x, pre.y * pre.y), pot);  // as kick_points
       if (vrow && ok) pot += vrow[x];
       // mu = dt Im(conj(lam+) psi+) with psi+ = exp(-i th) pre equals
       // dt Im(conj(exp(+i th) lam+) pre): the rotated lam serves both
