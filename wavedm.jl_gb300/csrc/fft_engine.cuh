@@ -263,6 +263,21 @@ __device__ __forceinline__ float2 twiddle_mul(float2 a, float4 w, bool inv) {
   return make_float2(fmaf(ax, w.x, fmaf(-ay, wy, cx)), fmaf(ay, w.x, fmaf(ax, wy, cy)));
 }
 
+// Tuning variant (WDM_FFT_TW_PLAIN): the stages multiply by the FP32 nearest
+// twiddle alone (a plain complex product), leaving out the remainder terms.
+template <bool ROT>
+__device__ __forceinline__ float2 stage_twiddle_mul(float2 a, float4 w, bool inv) {
+#if defined(WDM_FFT_TW_PLAIN)
+  const bool rot = ROT && (__float_as_uint(w.w) & 1u) != 0;
+  const float ax = rot ? (inv ? -a.y : a.y) : a.x;
+  const float ay = rot ? (inv ? a.x : -a.x) : a.y;
+  const float wy = inv ? -w.y : w.y;
+  return make_float2(fmaf(ax, w.x, -ay * wy), fmaf(ax, wy, ay * w.x));
+#else
+  return twiddle_mul<ROT>(a, w, inv);
+#endif
+}
+
 // Stage twiddles are laid out per stage as [jm][k-1] (jm < NS, 1 <= k < R),
 // stage after stage in the plan's radix order: stage s starts at OFF = sum of
 // NS (R - 1) over the earlier stages (N - 1 entries in all).  Lanes that run
@@ -279,7 +294,7 @@ __device__ __forceinline__ void stage_compute(float2* v, const float4* __restric
       const int jm = j % NS;
       const float4* w = tw + OFF + jm * (R - 1);
 #pragma unroll
-      for (int k = 1; k < R; ++k) v[i * R + k] = twiddle_mul<(NS * R) % 12 == 0>(v[i * R + k], w[k - 1], INV);
+      for (int k = 1; k < R; ++k) v[i * R + k] = stage_twiddle_mul<(NS * R) % 12 == 0>(v[i * R + k], w[k - 1], INV);
     }
     dftR<R, INV>(v + i * R);
   }
@@ -299,8 +314,8 @@ __device__ __forceinline__ void stage_compute2(float2* va, float2* vb, const flo
 #pragma unroll
       for (int k = 1; k < R; ++k) {
         const float4 wk = w[k - 1];
-        va[i * R + k] = twiddle_mul<(NS * R) % 12 == 0>(va[i * R + k], wk, INV);
-        vb[i * R + k] = twiddle_mul<(NS * R) % 12 == 0>(vb[i * R + k], wk, INV);
+        va[i * R + k] = stage_twiddle_mul<(NS * R) % 12 == 0>(va[i * R + k], wk, INV);
+        vb[i * R + k] = stage_twiddle_mul<(NS * R) % 12 == 0>(vb[i * R + k], wk, INV);
       }
     }
     dftR<R, INV>(va + i * R);
