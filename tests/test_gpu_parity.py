@@ -267,6 +267,35 @@ def test_cic_interpolation_matches_oracle(wdm):
     assert np.abs(got - ref).max() < 1e-5 * np.abs(ref).max()
 
 
+def test_particles_replaced_and_removed_between_calls(wdm):
+    """The CIC deposit is made once per particle set and kept: replacing the
+    particles between calls clears it and deposits the new set, and removing
+    them leaves no baryon density behind (each call against the FP64 oracle run
+    with that call's particles)."""
+    n, L, dt, k = (32, 24, 16), (8.0, 6.0, 4.0), 0.01, 3
+    g = spe.Grid(n, L)
+    X, Y, Z = g.coords()
+    rng = np.random.default_rng(12)
+    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 2) * np.exp(0.3j * rng.standard_normal((16, 24, 32)))).astype(
+        np.complex64)
+    sets = [(rng.uniform(-3.0, 3.0, (40, 3)), rng.uniform(0.01, 0.05, 40)),
+            (rng.uniform(-2.0, 2.0, (25, 3)), rng.uniform(0.02, 0.08, 25)),
+            None]
+    ref = psi0.astype(np.complex128)
+    with wdm.SPEContext(n, L, poisson_coeff=1.0) as ctx:
+        ctx.set_psi(psi0)
+        for parts in sets:
+            if parts is None:
+                ctx.set_particles(np.zeros((0, 3)), np.zeros(0))
+                phys = spe.Physics(poisson_coeff=1.0)
+            else:
+                ctx.set_particles(*parts)
+                phys = spe.Physics(poisson_coeff=1.0, rho_b=spe.cic_deposit(g, *parts))
+            ctx.step(k, dt)
+            ref = spe.run(ref, g, phys, dt, k)
+            assert spe.rel_l2(ctx.get_psi(), ref) < 2e-5
+
+
 def test_nonfinite_is_reported(wdm):
     from wavedm_gb300._abi import WdmError
 

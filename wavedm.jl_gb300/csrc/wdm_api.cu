@@ -1096,7 +1096,12 @@ wdm_status wdm_set_particles(wdm_ctx* c, const double* pos, const double* mass, 
     WDM_CU(c, cudaMemsetAsync(c->rb_rows, 0, sizeof(int) * c->d.ny * c->d.nz, c->st));
     c->rb_ready = 0;
   }
-  if (n == 0) return WDM_OK;
+  if (n == 0) {  // no baryons from now on: the potential and the density shift lose them too
+    c->rho_b_mean = 0.0;
+    if (c->have_psi) WDM_TRY(update_shift(c));
+    c->phi_valid = 0;
+    return WDM_OK;
+  }
   if (!pos || !mass) return fail(c, WDM_ERR_INVALID, "null particle arrays");
   if (!c->rho_b) {
     WDM_TRY(dalloc(c, &c->rho_b, (size_t)c->ncell));
