@@ -31,13 +31,14 @@ namespace wdm {
 // Stockham scatter of radix R at stride NS) and the next stage's read pattern
 // for the 32 lanes of a warp (8-byte words, 16 lanes per wavefront).  The
 // candidates are a padding p + (p >> s) (code s = 2..6; 30: none) and an XOR
-// swizzle of W bits at bit B by the W bits above them,
-// p ^ (((p >> (B + W)) & (2^W - 1)) << B) (code 100 + 10 W + B), which
-// permutes p within its aligned block of 2^(B + W) words and so needs no room
-// beyond the line.
+// swizzle of W bits at bit B by the W bits at bit A >= B + W,
+// p ^ (((p >> A) & (2^W - 1)) << B) (code 100 + 100 (A - B - W) + 10 W + B),
+// which permutes p within its aligned block of 2^(B + W) words and so needs
+// no room beyond the line.
 __host__ __device__ constexpr int xaddr(int p, int code) {
-  return code < 100 ? p + (p >> code)
-                    : (p ^ (((p >> (code % 10 + (code / 10) % 10)) & ((1 << ((code / 10) % 10)) - 1)) << (code % 10)));
+  if (code < 100) return p + (p >> code);
+  const int b = code % 10, w = (code / 10) % 10, a = b + w + (code - 100) / 100;
+  return p ^ (((p >> a) & ((1 << w) - 1)) << b);
 }
 
 // Largest number of distinct words that share a bank pair among 16 lane
@@ -84,35 +85,49 @@ struct XPad {
         }
     return total;
   }
-  // the cheapest map; on a tie the one needing the least room (no padding,
-  // then a swizzle, then the smallest padding)
-  __host__ __device__ static constexpr int best(int R, int NS, int RN) {
-    int bs = 30, bc = cost(R, NS, RN, 30);
-    for (int w = 2; w <= 3; ++w)
-      for (int b = 0; b <= 3; ++b) {
-        if (N % (1 << (b + w)) != 0) continue;
-        const int code = 100 + 10 * w + b;
-        const int c = cost(R, NS, RN, code);
-        if (c < bc) {
-          bc = c;
-          bs = code;
-        }
-      }
-    for (int sh = 6; sh >= 2; --sh) {
-      const int c = cost(R, NS, RN, sh);
-      if (c < bc) {
-        bc = c;
-        bs = sh;
-      }
-    }
-    return bs;
-  }
 };
 
-// The map of one stage boundary, evaluated once per boundary.
+// Candidate maps in order of preference on a tie: no padding, the paddings
+// s = 6..2 that fit below NP words, the swizzles (A - B - W = 0..3, then
+// W = 2, 3, 1, then B = 0..3).  A candidate that does not apply stands in as
+// no padding.
+constexpr int XCAND = 1 + 5 + 48;
+template <int N, int NP>
+__host__ __device__ constexpr int xcand(int i) {
+  if (i == 0) return 30;
+  if (i <= 5) {
+    const int sh = 7 - i;
+    return xaddr(N - 1, sh) < NP ? sh : 30;
+  }
+  const int j = i - 6, gap = j / 12, w = (j / 4) % 3 == 2 ? 1 : 2 + (j / 4) % 3, b = j % 4;
+  return N % (1 << (b + w)) == 0 ? 100 + 100 * gap + 10 * w + b : 30;
+}
+
+// Each candidate's cost is its own constant evaluation (one search over all of
+// them would exceed the compiler's budget for a single evaluation).
+template <int N, int T, int NP, int R, int NS, int RN, int CODE>
+struct XCost {
+  static constexpr int value = XPad<N, T, NP>::cost(R, NS, RN, CODE);
+};
+
+template <int N, int T, int NP, int R, int NS, int RN, int I = 0>
+struct XBest {
+  using Rest = XBest<N, T, NP, R, NS, RN, I + 1>;
+  static constexpr int here = xcand<N, NP>(I);
+  static constexpr int here_cost = XCost<N, T, NP, R, NS, RN, here>::value;
+  static constexpr int code = here_cost <= Rest::cost ? here : Rest::code;
+  static constexpr int cost = here_cost <= Rest::cost ? here_cost : Rest::cost;
+};
+template <int N, int T, int NP, int R, int NS, int RN>
+struct XBest<N, T, NP, R, NS, RN, XCAND> {
+  static constexpr int code = 30;
+  static constexpr int cost = 1 << 30;
+};
+
+// The map of one stage boundary (group buffers NP words apart).
 template <int N, int T, int NP, int R, int NS, int RN>
 struct XMap {
-  static constexpr int code = XPad<N, T, NP>::best(R, NS, RN);
+  static constexpr int code = XBest<N, T, NP, R, NS, RN>::code;
 };
 
 // Words one group's exchange buffer needs for the maps of the stage
@@ -249,6 +264,23 @@ struct XPlan<384> {
 #endif
 };
 
+// Group pitch of the exchange buffers where a warp holds several groups: the
+// pitch in N .. N + N/4 + 1 with the lowest total bank cost over the plan's
+// stage boundaries, each with its best map (a search over those pitches with
+// the bank simulation of XPad; every listed plan is conflict-free with it).
+// Other sizes take N + N/4 + 1.
+template <int N>
+struct XPitch {
+  static constexpr int value = N + N / 4 + 1;
+};
+template <> struct XPitch<12> { static constexpr int value = 14; };
+template <> struct XPitch<16> { static constexpr int value = 20; };
+template <> struct XPitch<24> { static constexpr int value = 26; };
+template <> struct XPitch<32> { static constexpr int value = 36; };
+template <> struct XPitch<48> { static constexpr int value = 52; };
+template <> struct XPitch<64> { static constexpr int value = 72; };
+template <> struct XPitch<96> { static constexpr int value = 104; };
+
 template <int N>
 struct XCfg {
   static constexpr int T = XPlan<N>::T;
@@ -257,10 +289,9 @@ struct XCfg {
   static constexpr int WARPS = 4;                      // warps per CTA
   static constexpr int NT = 32 * WARPS;
   // exchange buffer per group: with one group per warp only the maps' room
-  // (xextent); with several, a pitch of N + N/4 + 1 (odd), which the maps
-  // were chosen for
+  // (xextent); with several, the pitch XPitch, which the maps are chosen for
   static constexpr int NP0 = N + N / 4 + 1;
-  static constexpr int NP = GROUPS == 1 ? xextent<N, T, NP0>(typename XPlan<N>::Fwd{}) : NP0;
+  static constexpr int NP = GROUPS == 1 ? xextent<N, T, NP0>(typename XPlan<N>::Fwd{}) : XPitch<N>::value;
 #if defined(WDM_XTW_GLOBAL)
   static constexpr size_t TW_BYTES = 0;  // twiddles read from global memory (L1), not staged
 #else
