@@ -132,8 +132,10 @@ wdm_status wdm_set_tidal_clock(wdm_ctx* ctx, double t_first, double t_step);
  * wdm_adjoint refuses modes 1 and 2 (WDM_ERR_UNSUPPORTED). */
 typedef enum { WDM_TIDE_BOX_CENTRE = 0, WDM_TIDE_REFERENCE = 1, WDM_TIDE_DENSITY_MAX = 2 } wdm_tide_centering;
 wdm_status wdm_set_tidal_centering(wdm_ctx* ctx, int32_t mode);
-/* baryon particles (positions [n][3] and masses [n], doubles), CIC-deposited
- * into the density before every Poisson solve; n == 0 removes them. */
+/* static baryon particles (positions [n][3] and masses [n], doubles): their
+ * CIC deposit is made once, at the next density pass, and added to the density
+ * of every Poisson solve until the next call; n == 0 removes them.  The call
+ * invalidates the potential, which the next kick or step recomputes. */
 wdm_status wdm_set_particles(wdm_ctx* ctx, const double* pos, const double* mass, int64_t n);
 
 /* the path ------------------------------------------------------------------ */

@@ -196,7 +196,8 @@ K(dt/2) D(dt) iteration when KDK_flag is true, as the reference's loop does;
 * `kappa`: the local term kappa |psi|^2; `absorb_coeff`: the tanh absorbing mask.
 * `tidal`: a function t -> (Txx, Tyy, Tzz, Txy, Txz, Tyz) of the tidal tensor,
   sampled once per step on a clocked schedule; `tidal_centering` as set_tidal_centering!.
-* `particles`: (pos 3 x n, mass n) baryons, CIC-deposited every step.
+* `particles`: (pos 3 x n, mass n) static baryons, CIC-deposited once and added to the
+  density of every Poisson solve.
 * `outputdir`: writes "<title>, <suffix> - Prop.jld2" with the keys of
   save_evolution_results (src/io/save.jl:25-34) through JLD2, and the property
   table "<title>, <suffix> - Prop.csv" (src/io/save.jl:41-72).

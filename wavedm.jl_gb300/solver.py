@@ -146,7 +146,7 @@ def SPE3D_waveDM(*, Nx=64, Ny=None, Nz=None, Xmax=10.0, Ymax=None, Zmax=None, Nt
     literal K(dt/2) D(dt) iteration, the default when KDK_flag is true as in
     simulation_main.jl:538) or "lie" (KDK_flag false).  tidal: callable t ->
     (Txx, Tyy, Tzz, Txy, Txz, Tyz) for the 1/2 x^T T x tide.  particles:
-    (pos [n,3], mass [n]) CIC-deposited each step.  Returns a dict with psi, t,
+    (pos [n,3], mass [n]) CIC-deposited once (static).  Returns a dict with psi, t,
     dt and the per-snapshot diagnostics of the reference loop (wdm_diagnostics:
     mass, density maximum and its index, the radii R1..R9 about it, R, virial
     and momentum sums, timestep limits).  With outputdir, writes the
