@@ -213,7 +213,8 @@ struct Launch {
   // even pitch nx/2 + 2), and units of GROUPS row pairs inside one batch item.
   using XS = XStage<N>;
   static bool x_staged_ok(const RowGeom& rg, long long hpitch, const void* p0, const void* p1, const void* p2) {
-    if (rg.impl != X_IMPL_STAGED || hpitch != XS::HP || rg.pitch != N) return false;
+    // the staged copies take XS::HP entries of an H row (the pitch may be wider, and even)
+    if (rg.impl != X_IMPL_STAGED || hpitch < XS::HP || hpitch % 2 != 0 || rg.pitch != N) return false;
     if ((rg.nrows / 2) % XCfg<N>::GROUPS != 0 || rg.nrows % 2 != 0) return false;
     for (const void* p : {p0, p1, p2})
       if (reinterpret_cast<uintptr_t>(p) % 16) return false;

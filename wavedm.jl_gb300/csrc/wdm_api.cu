@@ -919,6 +919,10 @@ wdm_status wdm_create(const wdm_desc* d, wdm_ctx** out) {
   c->nxh = d->nx / 2 + 1;
   c->ncell = ncell;
   c->hpitch = c->nxh + (c->nxh & 1);
+#ifdef WDM_HPITCH_ALIGN
+  // tuning variant: rows of H start on WDM_HPITCH_ALIGN-element boundaries
+  c->hpitch = (c->nxh + WDM_HPITCH_ALIGN - 1) / WDM_HPITCH_ALIGN * WDM_HPITCH_ALIGN;
+#endif
   c->nhalf = (long long)c->hpitch * d->ny * d->nz;
   c->kx = kernels_for(d->nx);
   c->ky = kernels_for(d->ny);
