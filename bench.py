@@ -191,6 +191,9 @@ def workload_config(wl, args, world):
     return {"workload": wl["name"], "grid": [N, N, N], "box": wl["L"], "dt": wl["dt"], "mode": args.mode,
             "phase_mode": args.phase, "tidal": wl["tidal"] is not None,
             "baryon_particles": 0 if wl["particles"] is None else len(wl["particles"][1]),
+            "baryons": None if wl["particles"] is None else
+            "static: one CIC deposit before the timed steps, added to the density of every step's Poisson solve "
+            "(the reference computes the static baryons' potential once, src/simulation_main.jl:248-261)",
             "l2": "inputs larger than L2 (psi 8 B/cell)", "parallelism": f"replicas x{world}"}
 
 
