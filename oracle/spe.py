@@ -1,6 +1,6 @@
 """FP64 CPU restatement of WaveDM.jl's split-step Fourier KDK path (the oracle).
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker that the CUDA library is
+TEST INFRASTRUCTURE ONLY.  This module is the oracle that the CUDA library is
 compared against; it is imported by ``tests/``, by ``__graft_entry__.smoke()``
 and by the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py``.  The
 product path (``wavedm.jl_gb300``) never imports it.

@@ -92,7 +92,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 // host side
 // ---------------------------------------------------------------------------
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda
-// link); null when the driver does not provide it.
+// link); null when the installed CUDA driver does not provide it.
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void* p = nullptr;
