@@ -70,8 +70,9 @@ cudaError_t launch_mean_shift(const void* data, bool complex_in, long long n, in
 cudaError_t launch_reduce(const float2* psi, const float* phi, const RedGeom& g, double* partials, int nblocks,
                           int batch, cudaStream_t st);
 // CIC deposit of the particles into rho, which must be zero; rows (ny * nz
-// ints, may be null) flags the x rows that hold deposited mass.  The density
-// pass that reads the deposit zeroes the flagged rows and resets their flags.
+// ints, may be null) flags the x rows that hold deposited mass.  The deposit
+// of static particles is kept: every density pass reads its flagged rows, and
+// it is cleared only when the particles change.
 cudaError_t launch_cic_deposit(float* rho, const CicParticle* p, long long n, int nx, int ny, int nz, int* rows,
                                cudaStream_t st);
 cudaError_t launch_cic_interp(const float* field, const CicParticle* p, long long n, int nx, int ny, int nz,
