@@ -9,9 +9,9 @@
 // registers the warp's lane 0 issues the bulk copies of the same rows of its
 // next unit into it, so those copies run under the transforms of the current
 // unit.  Each row is one copy into a slot row whose pitch is padded by 16
-// bytes, so that the lane groups of a warp read different banks.  The slots
-// cost occupancy (3 CTAs of 4 warps per SM at N = 384) but leave each thread
-// up to 168 registers.  Every wait is bounded: a warp that gives up records
+// bytes, so that the lane groups of a warp read different banks.  At N = 384
+// the kernels run 3 CTAs of 4 warps per SM with up to 170 registers per
+// thread (XStageCap).  Every wait is bounded: a warp that gives up records
 // WDM_DEVERR_TMA_WAIT, drains its copies (bounded) and exits.
 #pragma once
 #include "xpass_warp.cuh"
