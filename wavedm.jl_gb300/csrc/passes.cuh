@@ -2,18 +2,21 @@
 //
 // Storage (x fastest, the C-order view of Julia's psi[x, y, z]):
 //   psi  complex64 [nz][ny][nx]        the wavefunction; every pass runs in place
-//   H    complex64 [nz][ny][nxh]       nxh = nx/2 + 1: the density / potential
-//                                      half spectrum along x (Hermitian in kx)
-// One KDK step is eight launches, each one read + one write of its array:
-//   P1 k_x_kick_fwd   H -> Phi rows (C2R), psi <- exp(-i dt Phi) psi, x-FFT fwd
-//   P2 k_lfft<fwd>    psi, y axis
-//   P3 k_lfft_mid     psi, z axis: fwd, exp(-i k^2 dt/2)/(nx ny nz), inverse
-//   P4 k_lfft<inv>    psi, y axis
-//   P5 k_x_inv_rho    psi x-FFT inverse (+ absorbing mask), rho = |psi|^2 (+ rho_b),
-//                     rho rows R2C -> H
-//   P6 k_lfft<fwd>    H, y axis
-//   P7 k_lfft_mid     H, z axis: fwd, -c/(k^2 nx ny nz), inverse
-//   P8 k_lfft<inv>    H, y axis
+//   H    complex64 [nz][ny][hpitch]    the density / potential half spectrum
+//                                      along x (nx/2 + 1 columns, Hermitian in
+//                                      kx; hpitch: that rounded up to even)
+// One KDK step is eight launches, each one read + one write of its array (the
+// line passes are k_lfft_tma, or k_lfft_tile; the x passes the staged k_xs_*
+// kernels of xpass_staged.cuh, or the direct k_xw_* kernels of xpass_warp.cuh):
+//   P1 kick       H -> Phi rows (C2R), psi <- exp(-i dt Phi) psi, x-FFT fwd
+//   P2 line <0>   psi, y axis
+//   P3 line <2>   psi, z axis: fwd, exp(-i k^2 dt/2)/(nx ny nz) (DriftOp), inverse
+//   P4 line <1>   psi, y axis
+//   P5 inv_rho    psi x-FFT inverse (+ absorbing mask), rho = |psi|^2 (+ rho_b),
+//                 rho rows R2C -> H
+//   P6 line <0>   H, y axis
+//   P7 line <2>   H, z axis: fwd, -c/(k^2 nx ny nz) (PoissonOp), inverse
+//   P8 line <1>   H, y axis
 #pragma once
 #include "fft_engine.cuh"
 #include "tma.cuh"
@@ -565,6 +568,7 @@ struct RhoArgs {
 };
 
 // ----------------------------------------------------------------------------
+// Arguments of the kick passes
 // ----------------------------------------------------------------------------
 struct KickArgs {
   float dt_hi, dt_lo;    // kick time step as a float pair (dt = hi + lo)
