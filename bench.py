@@ -46,17 +46,23 @@ TRAFFIC_FILE = os.path.join(ROOT, "profiles", "step384_traffic.json")
 CSRC = os.path.join(ROOT, "wavedm.jl_gb300", "csrc")
 
 
-def kernel_source_hash():
+def kernel_source_hash(csrc=None):
     """sha256 (first 16 hex digits) of the kernel sources (every csrc file but the
-    host-only pipeline wdm_api.cu), the key a traffic capture is valid for."""
+    host-only pipeline wdm_api.cu) with comments and blank space removed, the key a
+    traffic capture is valid for (an edit of a comment does not change it)."""
     import hashlib
+    import re
 
+    csrc = csrc or CSRC
     h = hashlib.sha256()
-    for f in sorted(os.listdir(CSRC)):
+    for f in sorted(os.listdir(csrc)):
         if f.endswith((".cu", ".cuh", ".h")) and f != "wdm_api.cu":
             h.update(f.encode())
-            with open(os.path.join(CSRC, f), "rb") as fh:
-                h.update(fh.read())
+            with open(os.path.join(csrc, f), encoding="utf-8") as fh:
+                text = fh.read()
+            text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+            text = re.sub(r"//[^\n]*", " ", text)
+            h.update(" ".join(text.split()).encode())
     return h.hexdigest()[:16]
 
 
