@@ -114,6 +114,21 @@ struct Launch {
     return encode_map_c64(map, data, dims, strides, box);
   }
 
+  template <int MODE, bool LATE, class Op>
+  static cudaError_t ltma_launch(float2* data, const CUtensorMap& map, const CUtensorMap& emap, const LineGeom& ge,
+                                 const float4* tw, const Op& op, int batch, cudaStream_t st) {
+    constexpr size_t SMEM = ltma_smem_bytes<N, MODE>();
+    cudaError_t e;
+    if ((e = prep_once<k_lfft_tma<N, MODE, Op, LATE>>(SMEM)) != cudaSuccess) return e;
+    const int tx = ge.edge ? ge.nxa / LINES : (ge.nxa + LINES - 1) / LINES;
+    const long long tiles = ((long long)ge.rows * tx + ge.edge) * batch;
+    const long long cap = (long long)resident_ctas<k_lfft_tma<N, MODE, Op, LATE>>(NT, SMEM) * sm_count();
+    const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
+    k_lfft_tma<N, MODE, Op, LATE><<<grid, NT, SMEM, st>>>(data, map, emap, ge, tw, op, batch);
+    ++tl_kernel_launches;
+    return cudaGetLastError();
+  }
+
   // persistent line pass: one wave of resident CTAs walking all tiles
   template <int MODE, class Op>
   static cudaError_t lpipe(float2* data, const LineGeom& g, const float4* tw, const Op& op, int batch,
@@ -123,22 +138,27 @@ struct Launch {
     {
       CUtensorMap map, emap;
       if (g.impl == LINE_IMPL_TMA && line_map(&map, data, g, batch)) {
-        constexpr size_t SMEM = ltma_smem_bytes<N, MODE>();
-        cudaError_t e;
-        if ((e = prep_once<k_lfft_tma<N, MODE, Op>>(SMEM)) != cudaSuccess) return e;
         LineGeom ge = g;
         ge.edge = 0;
 #ifndef WDM_NO_EDGE_TILES
         if (edge_map(&emap, data, g, batch)) ge.edge = g.rows / 8;
 #endif
         if (!ge.edge) emap = map;  // not read
-        const int tx = ge.edge ? g.nxa / LINES : (g.nxa + LINES - 1) / LINES;
-        const long long tiles = ((long long)g.rows * tx + ge.edge) * batch;
-        const long long cap = (long long)resident_ctas<k_lfft_tma<N, MODE, Op>>(NT, SMEM) * sm_count();
-        const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
-        k_lfft_tma<N, MODE, Op><<<grid, NT, SMEM, st>>>(data, map, emap, ge, tw, op, batch);
-        ++tl_kernel_launches;
-        return cudaGetLastError();
+        // The next tile's copy goes out late (k_lfft_tma) in the fused z
+        // passes, which are bound by instruction issue, and in the y passes
+        // of a half spectrum (the ones with edge tiles); early in the y passes
+        // of psi, which are bound by memory.  Measured at 384^3 against early
+        // everywhere: the z passes 0.8-1.1% faster, the half-spectrum y
+        // passes 1.3-3% faster; late everywhere made the psi y passes 0.7-1.3%
+        // slower.
+        if constexpr (MODE == 2) {
+          return ltma_launch<MODE, true>(data, map, emap, ge, tw, op, batch, st);
+        } else {
+#ifndef WDM_TMA_EARLY_HALF_Y  // tuning variant: early in every y pass
+          if (ge.edge) return ltma_launch<MODE, true>(data, map, emap, ge, tw, op, batch, st);
+#endif
+          return ltma_launch<MODE, false>(data, map, emap, ge, tw, op, batch, st);
+        }
       }
     }
 #endif

@@ -458,7 +458,7 @@ __host__ __device__ constexpr int ltma_min_blocks() {
   return ltma_smem_bytes<N, 2>() * 2 <= 220 * 1024 ? (threads_for<N>() * 2 <= 1024 ? 2 : 1) : 1;
 }
 
-template <int N, int MODE, class Op>
+template <int N, int MODE, class Op, bool LATE>
 __global__ void __launch_bounds__(threads_for<N>(), ltma_min_blocks<N>())
 k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap emap,
            LineGeom g, const float4* __restrict__ twg, Op op, int batch) {
@@ -476,15 +476,12 @@ k_lfft_tma(float2* __restrict__ data, const __grid_constant__ CUtensorMap map, c
   float* optab = reinterpret_cast<float*>(bar + 2);  // N entries (MODE 2)
   const int tid = threadIdx.x;
   const int l = tid % LINES, t = tid / LINES;
-  // When the copy of the next tile goes out.  The y passes (MODE 0 / 1) are
-  // bound by memory: they issue it before waiting for the current tile, and a
-  // barrier closes every tile so that the copy after next may overwrite its
-  // slot.  The fused z passes (MODE 2) are bound by instruction issue: they
-  // issue it after the current tile's first barrier, by which every thread has
-  // finished the other slot's tile, and save the closing barrier.  Measured at
-  // 384^3 with the late issue everywhere: the z passes 1-3% faster (drift
-  // 0.301 -> 0.298 ms), the psi y passes 1.3% slower.
-  constexpr bool LATE = MODE == 2;
+  // When the copy of the next tile goes out (LATE, chosen by the launcher).
+  // Early: before the wait for the current tile, so that two copies are in
+  // flight during the wait, and a barrier closes every tile so that the copy
+  // after next may overwrite its slot.  Late: after the current tile's first
+  // barrier, by which every thread has finished the other slot's tile, which
+  // saves the closing barrier.
   // tiles of 16 columns; when 16 does not divide nxa the last tile of a row
   // reaches past the tensor (zero-filled by the copy, not stored), unless the
   // last column goes to edge tiles

@@ -260,7 +260,7 @@ k_xs_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
   // of a unit instead of stalling the copies and the density.
   auto rb_mask = [&](long long uu) -> unsigned {
     if (!with_rb) return 0u;
-    if (!a.rb_rows) return (1u << S::ROWS) - 1u;
+    if (!a.rb_rows) return S::ROWS >= 32 ? ~0u : (1u << (S::ROWS & 31)) - 1u;
     int b, ra0;
     unit_rows(uu, C::GROUPS, ppi, &b, &ra0);
     unsigned m = 0;

@@ -625,6 +625,7 @@ k_xw_kick(const float2* psi_in, float2* psi, const float2* __restrict__ H, RowGe
   // psi_in == psi runs in place; a separate psi_in keeps the input state
   WDM_XPASS_PROLOGUE
   (void)nunits;
+  (void)t;
   xw_kick_units<N, FWD>(psi_in, psi, H, rg, hpitch, hbstride, a, w,
                         XSlice{(long long)blockIdx.x * C::WARPS + warp, wstride, tw, buf});
 }
@@ -762,6 +763,7 @@ k_xw_inv_rho(float2* __restrict__ psi, float2* __restrict__ H, RowGeom rg, long 
              const float4* __restrict__ twg, RhoArgs a, XWork w) {
   WDM_XPASS_PROLOGUE
   (void)nunits;
+  (void)t;
   xw_inv_rho_units<N, CEN>(psi, H, rg, hpitch, hbstride, a, w,
                            XSlice{(long long)blockIdx.x * C::WARPS + warp, wstride, tw, buf});
 }
