@@ -204,10 +204,10 @@ wdm_status wdm_fft3d(wdm_ctx* ctx, void* data_dev, int32_t dir);
  * (nx/2+1)*ny*nz <= 1,064,960 (a 128^3 grid), larger ones return
  * WDM_ERR_INVALID.  rho and phi are float32 device pointers [nz][ny][nx]; stream is
  * a cudaStream_t (NULL: the default stream).  The call synchronises that stream
- * before it returns, so phi is ready on return.
- * The first call on a device looks up the array's device address once, so make
- * that first call before any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU race and must be serialised by the caller.
+ * before it returns, so phi is ready on return, and for the same reason no call
+ * can be made while the stream is being captured into a CUDA graph.  All calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller.
  * It builds its twiddle tables on the device (FP64 sincospi) where wdm_poisson
  * builds them on the host, and it always takes the register-tile line passes
  * and the direct x passes, so its phi agrees with wdm_poisson's to FP32
